@@ -1,0 +1,205 @@
+/*
+ * misa_gb300: GB300-native (sm_103a) EAM step for MISA-MD's lattice-indexed atom store.
+ *
+ * C ABI of libmisa_gb300.so. Plain pointers and sizes only; every entry point returns an mg_status
+ * (0 = success) and never throws. One context owns one CUDA stream on one GPU; a context is not
+ * thread-safe, distinct contexts are independent.
+ *
+ * The record exchanged with the host is the reference's AtomElement (src/atom/atom_element.h:18-41)
+ * on LP64: id u64, type i32 (atom_type: -1 INVALID, 0 Fe, 1 Cu, 2 Ni), 4 bytes padding, then
+ * x[3], v[3], f[3], rho, df as doubles: 104 bytes. Slot arrays use the reference's linear index
+ * (z * size_y + y) * size_x + x over the ghost-extended grid with doubled x
+ * (src/lattice/lattice.h:63-66, src/atom/atom_set.cpp:18-26).
+ */
+#ifndef MISA_GB300_H
+#define MISA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mg_atom_element {
+    uint64_t id;
+    int32_t type;
+    int32_t pad_;
+    double x[3];
+    double v[3];
+    double f[3];
+    double rho;
+    double df;
+} mg_atom_element;
+
+typedef int32_t mg_status;
+enum {
+    MG_OK = 0,
+    MG_ERR_ARG = 1,          /* bad argument (null pointer, size mismatch, unsupported box) */
+    MG_ERR_CUDA = 2,         /* a CUDA runtime call failed; see mg_last_error */
+    MG_ERR_POTENTIAL = 3,    /* setfl file missing or malformed, or potential not initialised */
+    MG_ERR_CAPACITY = 4,     /* inter-atom or ghost inter-atom list overflowed its capacity */
+    MG_ERR_OUT_OF_GRID = 5,  /* an index left the ghost-extended slot grid (atom too far out of the box) */
+    MG_ERR_STATE = 6         /* call out of order (e.g. simulate before prepare) */
+};
+
+enum { MG_PREC_FP64 = 0, MG_PREC_MIXED = 1 };
+
+/* Device-side error bits reported by mg_thermo / mg_last_device_error. */
+enum {
+    MG_DEVERR_INTER_OVERFLOW = 1,
+    MG_DEVERR_GHOST_OVERFLOW = 2,
+    MG_DEVERR_OUT_OF_GRID = 4,
+    MG_DEVERR_DISPLACED_OVERFLOW = 8,
+    MG_DEVERR_BAD_TYPE = 16
+};
+
+typedef struct mg_context mg_context;
+
+/* ---------------------------------------------------------------------------------------------
+ * Environment: replaces cuda_env_init / cuda_env_clean (src/arch/arch_imp.h:17-19, called from
+ * src/arch/arch_env.hpp:15-25). Selects the device for contexts created afterwards.
+ * ------------------------------------------------------------------------------------------- */
+mg_status mg_env_init(int32_t device);
+mg_status mg_env_clean(void);
+
+/* ---------------------------------------------------------------------------------------------
+ * Context: replaces cuda_domain_init(const comm::BccDomain*) (src/arch/arch_imp.h:21, called at
+ * src/simulation.cpp:126-128). One rank owning the whole periodic box: phase_space unit cells per
+ * dimension, ghost width ceil(cutoff_radius_factor)+1 (src/simulation.cpp:120), cutoff radius
+ * lattice_const * cutoff_radius_factor (src/atom.cpp:14-19). Every dimension must be at least
+ * 2 * ghost cells. precision: MG_PREC_FP64 or MG_PREC_MIXED. inter_capacity: maximum local
+ * inter-atom count (0 picks a default).
+ * ------------------------------------------------------------------------------------------- */
+mg_status mg_create(const int64_t phase_space[3], double lattice_const, double cutoff_radius_factor,
+                    int32_t precision, int64_t inter_capacity, mg_context **out);
+mg_status mg_destroy(mg_context *ctx);
+/* Last error message of the context (or of the last failed mg_create when ctx is NULL). */
+const char *mg_last_error(const mg_context *ctx);
+/* Slot grid: size_x (doubled), size_y, size_z, ghost_x (doubled), ghost_y, ghost_z. */
+mg_status mg_grid(const mg_context *ctx, int64_t out[6]);
+mg_status mg_set_precision(mg_context *ctx, int32_t precision);
+
+/* ---------------------------------------------------------------------------------------------
+ * Neighbour offsets: replaces cuda_nei_offset_init(const NeighbourIndex<AtomElement>*)
+ * (src/arch/arch_imp.h:23, called at src/simulation.cpp:141-143). The context builds its own
+ * tables at mg_create; this entry point checks the host's four tables against them (same entries,
+ * same order) and returns MG_ERR_ARG on any difference.
+ * ------------------------------------------------------------------------------------------- */
+mg_status mg_nei_offset_init(mg_context *ctx, const int64_t *full_even, const int64_t *full_odd, int32_t n_full,
+                             const int64_t *half_even, const int64_t *half_odd, int32_t n_half);
+/* Copies one of the context's tables out (which: 0 full-even, 1 full-odd, 2 half-even, 3 half-odd,
+ * 4 pruned-full-even, 5 pruned-full-odd). Returns the table length in *n. */
+mg_status mg_nei_offsets(const mg_context *ctx, int32_t which, int64_t *out, int32_t cap, int32_t *n);
+
+/* ---------------------------------------------------------------------------------------------
+ * Potential: replaces cuda_pot_init(eam*) (src/arch/arch_imp.h:25, called at src/simulation.cpp:207
+ * after interpolateFile). Either a setfl file, or the parsed tables (F[e][nrho], rho[e][nr],
+ * r*phi[pair][nr] for pairs i>=j in lower-triangle order). atomic_numbers map atom types
+ * Fe/Cu/Ni (keys 26/29/28, src/types/atom_types.h:61-73) to table elements.
+ * ------------------------------------------------------------------------------------------- */
+mg_status mg_pot_init_setfl(mg_context *ctx, const char *path);
+mg_status mg_pot_init_tables(mg_context *ctx, int32_t n_ele, const int32_t *atomic_numbers, int32_t nrho,
+                             double drho, int32_t nr, double dr, double cutoff, const double *F_tables,
+                             const double *rho_tables, const double *rphi_tables);
+/* Spline coefficients the context uses for one table (kind 0 F, 1 rho, 2 r*phi of pair (e1,e2)):
+ * 7 doubles per knot (c0, c1, c2, c3, d0, d1, d2). Returns the knot count in *n. */
+mg_status mg_pot_spline(const mg_context *ctx, int32_t kind, int32_t e1, int32_t e2, double *out, int32_t cap,
+                        int32_t *n);
+
+/* ---------------------------------------------------------------------------------------------
+ * The reference's per-phase accelerator hooks (src/arch/arch_imp.h:27-31), called from
+ * atom::latRho / latDf / latForce (src/atom.cpp:159-160, 293-294, 320-321) with the host AoS slot
+ * array of the whole ghost-extended grid. On return the host array holds:
+ *   rho_calc:   rho of every local slot = the full lattice-lattice density (periodic images
+ *               included); ghost-slot rho is left 0, so the reverse rho fold that follows adds 0.
+ *   df_calc:    df = F'(rho) of every local non-vacancy slot.
+ *   force_calc: f of every local slot = the full lattice-lattice force (ghost-slot f left 0).
+ * Ghost df must already hold the owners' df (the host's forward df exchange runs before
+ * force_calc, src/atom.cpp:123-137). cutoff_radius must equal the context's cutoff.
+ * ------------------------------------------------------------------------------------------- */
+mg_status mg_eam_rho_calc(mg_context *ctx, mg_atom_element *atoms, double cutoff_radius);
+mg_status mg_eam_df_calc(mg_context *ctx, mg_atom_element *atoms, double cutoff_radius);
+mg_status mg_eam_force_calc(mg_context *ctx, mg_atom_element *atoms, double cutoff_radius);
+
+/* ---------------------------------------------------------------------------------------------
+ * Resident state: the whole step of simulation::simulate (src/simulation.cpp:238-268) on the GPU,
+ * state kept in HBM between calls.
+ * ------------------------------------------------------------------------------------------- */
+/* Upload the slot array (n_slots records, reference index order) and the inter-atom list. */
+mg_status mg_upload(mg_context *ctx, const mg_atom_element *atoms, int64_t n_slots, const mg_atom_element *inter,
+                    int64_t n_inter);
+/* Download the slot array and the inter-atom list (list order); *n_inter receives the count. */
+mg_status mg_download(mg_context *ctx, mg_atom_element *atoms, int64_t n_slots, mg_atom_element *inter,
+                      int64_t inter_cap, int64_t *n_inter);
+/* Ghost inter atoms (type, x, df; other fields 0), list order. */
+mg_status mg_download_ghost_inter(mg_context *ctx, mg_atom_element *ghost, int64_t cap, int64_t *n_ghost);
+/* NewtonMotion::setTimestepLength (src/newton_motion.cpp:13-17), dt in ps. */
+mg_status mg_set_timestep(mg_context *ctx, double dt_ps);
+/* simulation::prepareForStart body (src/simulation.cpp:209-219): first ghost exchange, computeEam. */
+mg_status mg_prepare(mg_context *ctx);
+/* nsteps iterations of the loop body (src/simulation.cpp:241-265): firststep, decide, exchangeInter,
+ * borderInter, exchangeAtom, computeEam, secondstep. Asynchronous on the context stream unless
+ * sync != 0. The step sequence is captured once as a CUDA graph and replayed. */
+mg_status mg_simulate(mg_context *ctx, int64_t nsteps, int32_t sync);
+/* One phase of the loop body, for parity checks: 0 firststep, 1 decide, 2 exchangeInter,
+ * 3 borderInter, 4 exchangeAtom, 5 computeEam, 6 secondstep. */
+mg_status mg_phase(mg_context *ctx, int32_t phase);
+/* simulation::collisionStep (src/simulation.cpp:282-291): atom::setv on the slot at
+ * lat = (cell x, cell y, cell z, basis) (src/atom.cpp:475-494), exchanges, computeEam. */
+mg_status mg_collision_step(mg_context *ctx, const int32_t lat[4], const double dir[3], double energy_ev);
+/* configuration::rescale (src/system_configuration.cpp:321-346) with n_atoms for the degrees of freedom. */
+mg_status mg_rescale(mg_context *ctx, double t_set, uint64_t n_atoms);
+
+typedef struct mg_thermo_out {
+    double mvv;               /* sum m v^2 (src/system_configuration.cpp:296-319) */
+    double kinetic_energy;    /* mvv / 2 */
+    double potential_energy;  /* sum F(rho_i) + 1/2 sum phi_ij (extension; only when requested) */
+    double force_sum[3];      /* configuration::systemForce (src/system_configuration.cpp:8-24) */
+    int64_t n_inter;          /* local inter atoms */
+    int64_t n_ghost_inter;
+    int64_t n_vacancy;        /* INVALID local slots */
+    uint32_t device_errors;   /* MG_DEVERR_* bits accumulated since the last mg_clear_errors */
+    uint32_t pad_;
+} mg_thermo_out;
+/* Synchronises the stream. with_energy != 0 runs the per-atom energy pass (needs a preceding
+ * computeEam on the current positions, which mg_prepare / mg_simulate / mg_collision_step give). */
+mg_status mg_thermo(mg_context *ctx, int32_t with_energy, mg_thermo_out *out);
+/* Per-slot energies (n_slots doubles, 0 for vacancies and ghosts) and per-inter energies, from the
+ * last energy pass. */
+mg_status mg_download_energies(mg_context *ctx, double *per_slot, int64_t n_slots, double *per_inter,
+                               int64_t inter_cap);
+mg_status mg_clear_errors(mg_context *ctx);
+
+/* ---------------------------------------------------------------------------------------------
+ * Drop-in full step with host state (the end-to-end path): uploads the host slot array and
+ * inter-atom list, runs nsteps loop bodies on the GPU, downloads both back. The host arrays keep
+ * being the state of record, as in the reference's host loop.
+ * ------------------------------------------------------------------------------------------- */
+mg_status mg_step_host(mg_context *ctx, mg_atom_element *atoms, int64_t n_slots, mg_atom_element *inter,
+                       int64_t inter_cap, int64_t *n_inter, int64_t nsteps);
+
+/* ---------------------------------------------------------------------------------------------
+ * Wigner-Seitz mapping on the GPU (src/lattice/ws_utils.cpp:91-189), for indexing parity checks:
+ * for n positions (xyz interleaved) writes the ghost-extended nearest-site coordinates
+ * (3 int64 per point, doubled x), the box flags of ws::isOutBox and the sub-box linear index of
+ * ws::findNearLatIndexInSubBox (-1 when outside).
+ * ------------------------------------------------------------------------------------------- */
+mg_status mg_ws_map(mg_context *ctx, const double *xyz, int64_t n, int64_t *coords, uint32_t *flags,
+                    int64_t *index);
+
+/* Measured kernel times of the last mg_simulate call with timing enabled (ms per step per kernel). */
+mg_status mg_enable_timing(mg_context *ctx, int32_t on);
+mg_status mg_kernel_times(const mg_context *ctx, double *ms, int32_t cap, int32_t *n, const char **names);
+/* Number of kernel launches per loop-body step in the captured graph. */
+mg_status mg_launches_per_step(const mg_context *ctx, int32_t *n);
+/* CUDA stream of the context (a cudaStream_t), for callers timing on it. */
+void *mg_stream(const mg_context *ctx);
+/* Page-lock a host range (the caller's slot array) so mg_step_host / mg_upload / mg_download copy it
+ * by DMA; undo with mg_host_unregister before freeing it. */
+mg_status mg_host_register(void *ptr, uint64_t bytes);
+mg_status mg_host_unregister(void *ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

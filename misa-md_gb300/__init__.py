@@ -1,0 +1,377 @@
+"""misa_md_gb300: GB300-native EAM step for MISA-MD's lattice-indexed atom store.
+
+Python plumbing over the C ABI of libmisa_gb300.so (include/misa_gb300.h): ctypes bindings, a
+``Context`` per GPU state, and ``Simulation``, which mirrors the reference's ``simulation`` class
+(src/simulation.h: createDomain, createAtoms, prepareForStart, simulate, collisionStep) so callers of
+the reference's API find the same call order. All compute runs in the CUDA library; there is no CPU
+fallback: loading fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import importlib.util
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _load_sibling(name):
+    mod_name = f"misa_md_gb300.{name}"
+    if mod_name in sys.modules:
+        return sys.modules[mod_name]
+    spec = importlib.util.spec_from_file_location(mod_name, os.path.join(HERE, f"{name}.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[mod_name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+workloads = _load_sibling("workloads")
+build = _load_sibling("build")
+ATOM_DTYPE = workloads.ATOM_DTYPE
+
+PREC = {"fp64": 0, "mixed": 1}
+STATUS = {0: "MG_OK", 1: "MG_ERR_ARG", 2: "MG_ERR_CUDA", 3: "MG_ERR_POTENTIAL", 4: "MG_ERR_CAPACITY",
+          5: "MG_ERR_OUT_OF_GRID", 6: "MG_ERR_STATE"}
+
+
+class MgError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class ThermoOut(ctypes.Structure):
+    _fields_ = [("mvv", ctypes.c_double), ("kinetic_energy", ctypes.c_double),
+                ("potential_energy", ctypes.c_double), ("force_sum", ctypes.c_double * 3),
+                ("n_inter", ctypes.c_int64), ("n_ghost_inter", ctypes.c_int64), ("n_vacancy", ctypes.c_int64),
+                ("device_errors", ctypes.c_uint32), ("pad_", ctypes.c_uint32)]
+
+
+_LIB = None
+_P = ctypes.c_void_p
+_I32, _I64, _U64, _D = ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64, ctypes.c_double
+
+_PROTOS = {
+    "mg_env_init": (_I32, [_I32]),
+    "mg_env_clean": (_I32, []),
+    "mg_create": (_I32, [_P, _D, _D, _I32, _I64, _P]),
+    "mg_destroy": (_I32, [_P]),
+    "mg_last_error": (ctypes.c_char_p, [_P]),
+    "mg_grid": (_I32, [_P, _P]),
+    "mg_set_precision": (_I32, [_P, _I32]),
+    "mg_nei_offset_init": (_I32, [_P, _P, _P, _I32, _P, _P, _I32]),
+    "mg_nei_offsets": (_I32, [_P, _I32, _P, _I32, _P]),
+    "mg_pot_init_setfl": (_I32, [_P, ctypes.c_char_p]),
+    "mg_pot_init_tables": (_I32, [_P, _I32, _P, _I32, _D, _I32, _D, _D, _P, _P, _P]),
+    "mg_pot_spline": (_I32, [_P, _I32, _I32, _I32, _P, _I32, _P]),
+    "mg_eam_rho_calc": (_I32, [_P, _P, _D]),
+    "mg_eam_df_calc": (_I32, [_P, _P, _D]),
+    "mg_eam_force_calc": (_I32, [_P, _P, _D]),
+    "mg_upload": (_I32, [_P, _P, _I64, _P, _I64]),
+    "mg_download": (_I32, [_P, _P, _I64, _P, _I64, _P]),
+    "mg_download_ghost_inter": (_I32, [_P, _P, _I64, _P]),
+    "mg_set_timestep": (_I32, [_P, _D]),
+    "mg_prepare": (_I32, [_P]),
+    "mg_simulate": (_I32, [_P, _I64, _I32]),
+    "mg_phase": (_I32, [_P, _I32]),
+    "mg_collision_step": (_I32, [_P, _P, _P, _D]),
+    "mg_rescale": (_I32, [_P, _D, _U64]),
+    "mg_thermo": (_I32, [_P, _I32, _P]),
+    "mg_download_energies": (_I32, [_P, _P, _I64, _P, _I64]),
+    "mg_clear_errors": (_I32, [_P]),
+    "mg_step_host": (_I32, [_P, _P, _I64, _P, _I64, _P, _I64]),
+    "mg_ws_map": (_I32, [_P, _P, _I64, _P, _P, _P]),
+    "mg_enable_timing": (_I32, [_P, _I32]),
+    "mg_kernel_times": (_I32, [_P, _P, _I32, _P, _P]),
+    "mg_launches_per_step": (_I32, [_P, _P]),
+    "mg_stream": (_P, [_P]),
+    "mg_host_register": (_I32, [_P, _U64]),
+    "mg_host_unregister": (_I32, [_P]),
+}
+
+
+def library_path() -> str:
+    return build.LIB_PATH
+
+
+def load_library(build_if_missing: bool = False) -> ctypes.CDLL:
+    """Load libmisa_gb300.so; raises if it is not built (no fallback path exists)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = build.LIB_PATH
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"libmisa_gb300.so is not built ({path}); run __graft_entry__.build()")
+        build.build()
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in _PROTOS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def exported_symbols():
+    return list(_PROTOS)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def host_register(array):
+    """Page-lock a numpy array's memory for DMA copies (mg_host_register)."""
+    lib = load_library()
+    st = lib.mg_host_register(array.ctypes.data_as(ctypes.c_void_p), array.nbytes)
+    if st != 0:
+        raise MgError(st, (lib.mg_last_error(None) or b"").decode())
+
+
+def host_unregister(array):
+    lib = load_library()
+    st = lib.mg_host_unregister(array.ctypes.data_as(ctypes.c_void_p))
+    if st != 0:
+        raise MgError(st, (lib.mg_last_error(None) or b"").decode())
+
+
+class Context:
+    """One GPU state (mg_context): the ghost-extended slot grid of a periodic BCC box."""
+
+    def __init__(self, cells, lattice_const, cutoff_radius_factor, precision="fp64", inter_capacity=0,
+                 device=0):
+        self.lib = load_library()
+        self.cells = tuple(int(c) for c in cells)
+        self.lattice_const = float(lattice_const)
+        self.cutoff_radius_factor = float(cutoff_radius_factor)
+        self.precision = precision
+        self._check(self.lib.mg_env_init(device), None)
+        h = ctypes.c_void_p()
+        ps = np.asarray(self.cells, dtype=np.int64)
+        st = self.lib.mg_create(_ptr(ps), self.lattice_const, self.cutoff_radius_factor, PREC[precision],
+                                int(inter_capacity), ctypes.byref(h))
+        self._check(st, None)
+        self.h = h
+        g = np.zeros(6, dtype=np.int64)
+        self._check(self.lib.mg_grid(self.h, _ptr(g)))
+        self.grid = tuple(int(v) for v in g)
+        self.n_slots = int(g[0] * g[1] * g[2])
+
+    # ---- plumbing ----
+    def _check(self, status, h="self"):
+        if status != 0:
+            handle = self.h if h == "self" else None
+            msg = self.lib.mg_last_error(handle)
+            raise MgError(status, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def cutoff_radius(self):
+        return self.lattice_const * self.cutoff_radius_factor
+
+    # ---- setup ----
+    def pot_init_setfl(self, path):
+        self._check(self.lib.mg_pot_init_setfl(self.h, os.fsencode(path)))
+
+    def pot_spline(self, kind, e1, e2=0):
+        n = ctypes.c_int32()
+        self._check(self.lib.mg_pot_spline(self.h, kind, e1, e2, None, 0, ctypes.byref(n)))
+        out = np.zeros(7 * n.value)
+        self._check(self.lib.mg_pot_spline(self.h, kind, e1, e2, _ptr(out), out.size, ctypes.byref(n)))
+        return out.reshape(n.value, 7)
+
+    def nei_offsets(self, which):
+        n = ctypes.c_int32()
+        self._check(self.lib.mg_nei_offsets(self.h, which, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=np.int64)
+        self._check(self.lib.mg_nei_offsets(self.h, which, _ptr(out), out.size, ctypes.byref(n)))
+        return out
+
+    def nei_offset_init(self, full_even, full_odd, half_even, half_odd):
+        a = [np.ascontiguousarray(x, dtype=np.int64) for x in (full_even, full_odd, half_even, half_odd)]
+        self._check(self.lib.mg_nei_offset_init(self.h, _ptr(a[0]), _ptr(a[1]), len(a[0]), _ptr(a[2]),
+                                                _ptr(a[3]), len(a[2])))
+
+    def set_timestep(self, dt):
+        self._check(self.lib.mg_set_timestep(self.h, float(dt)))
+
+    def set_precision(self, precision):
+        self._check(self.lib.mg_set_precision(self.h, PREC[precision]))
+        self.precision = precision
+
+    # ---- state ----
+    def upload(self, atoms, inter=None):
+        atoms = np.ascontiguousarray(atoms, dtype=ATOM_DTYPE)
+        if atoms.size != self.n_slots:
+            raise ValueError(f"slot array has {atoms.size} records, grid has {self.n_slots}")
+        inter = np.zeros(0, dtype=ATOM_DTYPE) if inter is None else np.ascontiguousarray(inter, dtype=ATOM_DTYPE)
+        self._check(self.lib.mg_upload(self.h, _ptr(atoms), atoms.size, _ptr(inter) if inter.size else None,
+                                       inter.size))
+
+    def download(self, inter_cap=None):
+        atoms = np.zeros(self.n_slots, dtype=ATOM_DTYPE)
+        n = ctypes.c_int64()
+        self._check(self.lib.mg_download(self.h, _ptr(atoms), atoms.size, None, 0, ctypes.byref(n)))
+        cap = n.value if inter_cap is None else inter_cap
+        inter = np.zeros(cap, dtype=ATOM_DTYPE)
+        if cap:
+            self._check(self.lib.mg_download(self.h, _ptr(atoms), atoms.size, _ptr(inter), cap, ctypes.byref(n)))
+        return atoms, inter[:min(cap, n.value)]
+
+    def download_ghost_inter(self):
+        n = ctypes.c_int64()
+        self._check(self.lib.mg_download_ghost_inter(self.h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=ATOM_DTYPE)
+        if n.value:
+            self._check(self.lib.mg_download_ghost_inter(self.h, _ptr(out), n.value, ctypes.byref(n)))
+        return out
+
+    # ---- steps ----
+    def prepare(self):
+        self._check(self.lib.mg_prepare(self.h))
+
+    def simulate(self, steps, sync=True):
+        self._check(self.lib.mg_simulate(self.h, int(steps), 1 if sync else 0))
+
+    def phase(self, k):
+        self._check(self.lib.mg_phase(self.h, int(k)))
+
+    def collision_step(self, lat, direction, energy):
+        lat = np.asarray(lat, dtype=np.int32)
+        d = np.asarray(direction, dtype=np.float64)
+        self._check(self.lib.mg_collision_step(self.h, _ptr(lat), _ptr(d), float(energy)))
+
+    def rescale(self, t_set, n_atoms):
+        self._check(self.lib.mg_rescale(self.h, float(t_set), int(n_atoms)))
+
+    def thermo(self, with_energy=False):
+        out = ThermoOut()
+        self._check(self.lib.mg_thermo(self.h, 1 if with_energy else 0, ctypes.byref(out)))
+        return {"mvv": out.mvv, "kinetic_energy": out.kinetic_energy, "potential_energy": out.potential_energy,
+                "force_sum": tuple(out.force_sum), "n_inter": out.n_inter, "n_ghost_inter": out.n_ghost_inter,
+                "n_vacancy": out.n_vacancy, "device_errors": out.device_errors}
+
+    def energies(self, inter_cap=0):
+        per_slot = np.zeros(self.n_slots)
+        per_inter = np.zeros(inter_cap)
+        self._check(self.lib.mg_download_energies(self.h, _ptr(per_slot), per_slot.size,
+                                                  _ptr(per_inter) if inter_cap else None, inter_cap))
+        return per_slot, per_inter
+
+    # ---- reference hooks ----
+    def eam_rho_calc(self, atoms):
+        self._check(self.lib.mg_eam_rho_calc(self.h, _ptr(atoms), self.cutoff_radius))
+
+    def eam_df_calc(self, atoms):
+        self._check(self.lib.mg_eam_df_calc(self.h, _ptr(atoms), self.cutoff_radius))
+
+    def eam_force_calc(self, atoms):
+        self._check(self.lib.mg_eam_force_calc(self.h, _ptr(atoms), self.cutoff_radius))
+
+    def step_host(self, atoms, inter, n_inter, nsteps):
+        n = ctypes.c_int64(n_inter)
+        self._check(self.lib.mg_step_host(self.h, _ptr(atoms), atoms.size, _ptr(inter), inter.size,
+                                          ctypes.byref(n), int(nsteps)))
+        return n.value
+
+    # ---- utilities ----
+    def ws_map(self, xyz):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        n = xyz.shape[0]
+        coords = np.zeros((n, 3), dtype=np.int64)
+        flags = np.zeros(n, dtype=np.uint32)
+        index = np.zeros(n, dtype=np.int64)
+        self._check(self.lib.mg_ws_map(self.h, _ptr(xyz), n, _ptr(coords), _ptr(flags), _ptr(index)))
+        return coords, flags, index
+
+    def enable_timing(self, on=True):
+        self._check(self.lib.mg_enable_timing(self.h, 1 if on else 0))
+
+    def kernel_times(self):
+        n = ctypes.c_int32()
+        ms = np.zeros(32)
+        names = (ctypes.c_char_p * 32)()
+        self._check(self.lib.mg_kernel_times(self.h, _ptr(ms), 32, ctypes.byref(n), names))
+        return {names[k].decode(): float(ms[k]) for k in range(n.value)}
+
+    def launches_per_step(self):
+        n = ctypes.c_int32()
+        self._check(self.lib.mg_launches_per_step(self.h, ctypes.byref(n)))
+        return n.value
+
+    def stream(self):
+        return self.lib.mg_stream(self.h)
+
+
+class Simulation:
+    """Mirror of the reference's simulation class (src/simulation.h), one GPU owning the whole box.
+
+    createDomain -> create_domain, createAtoms -> create_atoms, prepareForStart -> prepare_for_start,
+    simulate -> simulate, collisionStep -> collision_step. Errors raise MgError instead of MPI_Abort.
+    """
+
+    def __init__(self, precision="fp64", inter_capacity=0):
+        self.precision = precision
+        self.inter_capacity = inter_capacity
+        self.ctx = None
+        self.phase_space = None
+
+    def create_domain(self, phase_space, lattice_const, cutoff_radius_factor):
+        self.phase_space = tuple(int(v) for v in phase_space)
+        self.lattice_const = float(lattice_const)
+        self.cutoff_radius_factor = float(cutoff_radius_factor)
+        self.ctx = Context(self.phase_space, lattice_const, cutoff_radius_factor, self.precision,
+                           self.inter_capacity)
+
+    def create_atoms(self, init_step_len, t_set, create_seed, alloy_ratio=(1.0, 0.0, 0.0), atoms=None):
+        """Create-mode state (WorldBuilder-style BCC crystal at t_set) unless a slot array is given."""
+        if atoms is None:
+            total = float(sum(alloy_ratio))
+            atoms = workloads.build_state(self.phase_space, self.lattice_const, self.cutoff_radius_factor,
+                                          temperature=t_set, seed=create_seed,
+                                          cu_frac=alloy_ratio[1] / total, ni_frac=alloy_ratio[2] / total)
+        self._atoms = atoms
+        self.ctx.set_timestep(init_step_len)
+
+    def prepare_for_start(self, pot_file_path):
+        self.ctx.pot_init_setfl(pot_file_path)
+        self.ctx.upload(self._atoms)
+        self._atoms = None
+        self.ctx.prepare()
+
+    def simulate(self, steps):
+        self.ctx.simulate(steps, sync=True)
+
+    def collision_step(self, coll_lat, coll_dir, pka_energy):
+        self.ctx.collision_step(coll_lat, coll_dir, pka_energy)
+
+    def set_timestep_length(self, dt):
+        self.ctx.set_timestep(dt)
+
+    def kinetic_energy(self):
+        return self.ctx.thermo()["kinetic_energy"]
+
+    def temperature(self):
+        n = 2 * self.phase_space[0] * self.phase_space[1] * self.phase_space[2]
+        return self.ctx.thermo()["mvv"] * workloads.MVV2E / ((3 * n - 3) * workloads.BOLTZ)

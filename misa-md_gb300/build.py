@@ -1,0 +1,68 @@
+"""Build recipe of libmisa_gb300.so: nvcc for sm_103a, translation units compiled in parallel.
+
+The host translation units (.cpp) go through nvcc to the host compiler with -ffp-contract=off so the
+spline coefficients round exactly as written; device code uses explicit rounding intrinsics where
+the reference's results must be reproduced bit for bit.
+"""
+from __future__ import annotations
+
+import concurrent.futures
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libmisa_gb300.so")
+SOURCES = ["csrc/mg_kernels.cu", "csrc/mg_api.cpp", "csrc/mg_potential.cpp"]
+HEADERS = ["csrc/mg_internal.h", "../include/misa_gb300.h"]
+NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
+              "-Xcompiler", "-fPIC,-ffp-contract=off"]
+
+
+def nvcc() -> str:
+    path = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(path):
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libmisa_gb300.so")
+    return path
+
+
+def _stale() -> bool:
+    if not os.path.exists(LIB_PATH):
+        return True
+    t = os.path.getmtime(LIB_PATH)
+    files = SOURCES + HEADERS + [os.path.relpath(__file__, HERE)]
+    return any(os.path.getmtime(os.path.join(HERE, f)) > t for f in files)
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile the library if a source is newer than it; returns the library path."""
+    if not force and not _stale():
+        return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    cc = nvcc()
+    objs = []
+    cmds = []
+    for src in SOURCES:
+        obj = os.path.join(BUILD_DIR, os.path.splitext(os.path.basename(src))[0] + ".o")
+        objs.append(obj)
+        cmds.append([cc, *NVCC_FLAGS, "-c", "-o", obj, os.path.join(HERE, src)])
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("build failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+        return r.stdout + r.stderr
+
+    with concurrent.futures.ThreadPoolExecutor(len(cmds)) as ex:
+        for out in ex.map(run, cmds):
+            if verbose and out.strip():
+                print(out)
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    run([cc, *NVCC_FLAGS, "-shared", "-o", tmp, *objs, "-lcudart"])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    print(build(force=True, verbose=True))

@@ -1,0 +1,930 @@
+// C ABI of libmisa_gb300.so: context lifetime, device state, potential upload, the per-step kernel
+// sequence (captured once as a CUDA graph), the reference's per-phase hooks and the thermo reductions.
+// The call order of one step follows simulation::simulate (src/simulation.cpp:238-268).
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mg_internal.h"
+
+using namespace mg;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+constexpr int kNumTimers = 12;
+const char *kTimerNames[kNumTimers] = {"firststep", "inter_firststep", "inter_manage", "ghost_copy",
+                                       "lat_rho",   "inter_rho",       "lat_df",       "ghost_df",
+                                       "lat_force", "inter_force",     "secondstep",   "far_scatter"};
+
+}  // namespace
+
+struct mg_context {
+    int device = 0;
+    int precision = MG_PREC_FP64;
+    Geom g{};
+    Slots s{};
+    Inter in{};
+    PotTables pt{};
+    bool pot_ready = false;
+    HostPotential hp;               // the spline coefficients in use
+    int types_ok_mask = 0;          // bit t set: the potential has the element of atom type t
+    std::vector<void *> dev_allocs;
+    void *pot_mem = nullptr;
+    OffsetTable offs;
+    std::vector<int> lat_order[2];  // reordered full table (pruned entries first), linear offsets
+    int n_full = 0, n_pruned = 0;
+    cudaStream_t stream = nullptr;
+    int num_sms = 1;
+    StepParams sp{};
+    double dt = 0.0;
+    bool prepared = false;
+    std::string err;
+    mg_atom_element *d_aos = nullptr;
+    double *d_partials = nullptr;
+    double *d_thermo = nullptr;
+    int n_partials = 0;
+    double *d_ws_xyz = nullptr;
+    int64_t *d_ws_coords = nullptr, *d_ws_index = nullptr;
+    uint32_t *d_ws_flags = nullptr;
+    int64_t ws_cap = 0;
+    cudaGraphExec_t graph_exec = nullptr;
+    double graph_dt = -1.0;
+    int graph_prec = -1;
+    int launches_per_step = 0;
+    bool timing = false;
+    std::vector<cudaEvent_t> ev;       // kNumTimers + 1 events per timed step
+    std::vector<double> timer_ms;      // accumulated per kernel
+    int64_t timed_steps = 0;
+    bool energy_valid = false;
+
+    LaunchCtx lc() const { return LaunchCtx{stream, num_sms}; }
+    bool mixed() const { return precision == MG_PREC_MIXED; }
+};
+
+#define MG_CK(call)                                                                             \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess) {                                                                \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                     \
+            return MG_ERR_CUDA;                                                                 \
+        }                                                                                       \
+    } while (0)
+
+namespace {
+
+template <class T>
+cudaError_t dalloc(mg_context *ctx, T **p, size_t n) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, n * sizeof(T) + 16);
+    if (e == cudaSuccess) {
+        ctx->dev_allocs.push_back(q);
+        *p = static_cast<T *>(q);
+    }
+    return e;
+}
+
+int next_pow2(int n) {
+    int p = 1;
+    while (p < n) p <<= 1;
+    return p;
+}
+
+mg_status check_launch(mg_context *ctx) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        ctx->err = std::string("kernel launch: ") + cudaGetErrorString(e);
+        return MG_ERR_CUDA;
+    }
+    return MG_OK;
+}
+
+void set_dt(mg_context *ctx, double dt) {  // NewtonMotion::preComputeDtInv2m (src/newton_motion.cpp:19-28)
+    ctx->dt = dt;
+    ctx->sp.dt = dt;
+    for (int i = 0; i < 3; i++) {
+        const double m = atom_mass(i);
+        const double dt_halve = 0.5 * dt * kFtm2v;
+        ctx->sp.dt_inv_m[i] = dt_halve / m;
+    }
+}
+
+// timer helpers (direct launches only)
+struct Timer {
+    mg_context *ctx;
+    int64_t step;
+    void mark(int k) {
+        if (!ctx->timing) return;
+        cudaEventRecord(ctx->ev[static_cast<size_t>(step) * (kNumTimers + 1) + k], ctx->stream);
+    }
+};
+
+// ---- the kernel sequences ----
+void seq_firststep(mg_context *ctx, bool decide, Timer *t) {
+    const LaunchCtx lc = ctx->lc();
+    launch_firststep(lc, ctx->g, ctx->s, ctx->in, ctx->sp, decide, ctx->mixed());
+    if (t) t->mark(1);
+    launch_inter_firststep(lc, ctx->in, ctx->sp);
+    if (t) t->mark(2);
+}
+void seq_compute_eam(mg_context *ctx, bool kick, bool with_manage_prefix, int manage_mask, Timer *t) {
+    const LaunchCtx lc = ctx->lc();
+    const bool mx = ctx->mixed();
+    if (with_manage_prefix) launch_inter_manage(lc, ctx->g, ctx->s, ctx->in, manage_mask | MANAGE_INDEX, mx);
+    else launch_inter_manage(lc, ctx->g, ctx->s, ctx->in, MANAGE_INDEX, mx);
+    if (t) t->mark(3);
+    launch_ghost_copy(lc, ctx->g, ctx->s, mx);
+    if (t) t->mark(4);
+    launch_lat_rho(lc, ctx->g, ctx->s, ctx->in, ctx->pt, mx, false);
+    if (t) t->mark(5);
+    launch_far_scatter(lc, ctx->g, ctx->s, ctx->in, ctx->pt, 0, mx);
+    launch_inter_rho(lc, ctx->g, ctx->s, ctx->in, ctx->pt, mx);
+    if (t) t->mark(6);
+    launch_lat_df(lc, ctx->g, ctx->s, ctx->in, ctx->pt, mx, false);
+    if (t) t->mark(7);
+    launch_ghost_df(lc, ctx->g, ctx->s, ctx->in, mx);
+    if (t) t->mark(8);
+    launch_lat_force(lc, ctx->g, ctx->s, ctx->in, ctx->pt, ctx->sp, kick, mx, false);
+    if (t) t->mark(9);
+    launch_far_scatter(lc, ctx->g, ctx->s, ctx->in, ctx->pt, 1, mx);
+    launch_inter_force(lc, ctx->g, ctx->s, ctx->in, ctx->pt, mx);
+    if (t) t->mark(10);
+    if (kick) launch_secondstep(lc, ctx->g, ctx->s, ctx->in, ctx->sp, false);
+    if (t) t->mark(11);
+}
+// one loop body: firststep, decide, exchangeInter, borderInter, exchangeAtom, computeEam, secondstep
+void seq_step(mg_context *ctx, Timer *t) {
+    if (t) t->mark(0);
+    seq_firststep(ctx, true, t);
+    seq_compute_eam(ctx, true, true, MANAGE_DECIDE | MANAGE_CLEAR_GHOST | MANAGE_EXCHANGE | MANAGE_BORDER, t);
+}
+constexpr int kLaunchesPerStep = 14;
+
+mg_status require_ready(mg_context *ctx) {
+    if (!ctx->pot_ready) { ctx->err = "potential not initialised"; return MG_ERR_POTENTIAL; }
+    return MG_OK;
+}
+
+mg_status ensure_aos(mg_context *ctx) {
+    if (ctx->d_aos) return MG_OK;
+    MG_CK(dalloc(ctx, &ctx->d_aos, static_cast<size_t>(ctx->g.n_slots)));
+    return MG_OK;
+}
+
+mg_status upload_tables(mg_context *ctx) {
+    std::vector<int> fe(ctx->n_full), fo(ctx->n_full);
+    for (int i = 0; i < ctx->n_full; i++) {
+        fe[i] = static_cast<int>(ctx->offs.off[0][i]);
+        fo[i] = static_cast<int>(ctx->offs.off[1][i]);
+    }
+    // reordered lattice tables; site_j - site_i in units of a0/2 = 2 * (vector in units of a0),
+    // small exact integers
+    std::vector<float> ds[2];
+    ds[0].resize(3 * ctx->n_full);
+    ds[1].resize(3 * ctx->n_full);
+    std::vector<int> le(ctx->n_full), lo(ctx->n_full);
+    for (int p = 0; p < 2; p++) {
+        std::vector<int> &dst = p ? lo : le;
+        for (int q = 0; q < ctx->n_full; q++) {
+            const int e = ctx->lat_order[p][q];
+            dst[q] = static_cast<int>(ctx->offs.off[p][e]);
+            for (int k = 0; k < 3; k++) ds[p][3 * q + k] = static_cast<float>(2.0 * ctx->offs.vec[p][3 * e + k]);
+        }
+    }
+    set_constant_tables(fe.data(), fo.data(), ctx->n_full, le.data(), lo.data(), ctx->n_pruned, ds[0].data(),
+                        ds[1].data(), ctx->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { ctx->err = std::string("constant tables: ") + cudaGetErrorString(e); return MG_ERR_CUDA; }
+    return MG_OK;
+}
+
+mg_status install_potential(mg_context *ctx, const HostPotential &hp) {
+    // element tables: double4 value + double4 derivative records, then float4 copies
+    const int ne = hp.n_ele, npair = ne * (ne + 1) / 2;
+    const size_t nr = hp.nr, nrho = hp.nrho;
+    const size_t n_rec = ne * nrho + ne * nr + npair * nr;  // records per table kind
+    std::vector<Knot64> vd(n_rec), dd(n_rec);
+    std::vector<float4> vf(n_rec), df(n_rec);
+    std::vector<size_t> base_F(ne), base_rho(ne), base_z(npair);
+    size_t at = 0;
+    auto put = [&](const HostSpline &sp) {
+        const size_t b = at;
+        for (int m = 0; m < sp.n; m++, at++) {
+            vd[at] = Knot64{sp.c0[m], sp.c1[m], sp.c2[m], sp.c3[m]};
+            dd[at] = Knot64{sp.d0[m], sp.d1[m], sp.d2[m], 0.0};
+            vf[at] = make_float4((float) sp.c0[m], (float) sp.c1[m], (float) sp.c2[m], (float) sp.c3[m]);
+            df[at] = make_float4((float) sp.d0[m], (float) sp.d1[m], (float) sp.d2[m], 0.0f);
+        }
+        return b;
+    };
+    for (int e = 0; e < ne; e++) base_F[e] = put(hp.F[e]);
+    for (int e = 0; e < ne; e++) base_rho[e] = put(hp.rho[e]);
+    for (int q = 0; q < npair; q++) base_z[q] = put(hp.z2[q]);
+    if (ctx->pot_mem) { cudaFree(ctx->pot_mem); ctx->pot_mem = nullptr; }
+    const size_t bytes = n_rec * (2 * sizeof(Knot64) + 2 * sizeof(float4));
+    MG_CK(cudaMalloc(&ctx->pot_mem, bytes));
+    Knot64 *d_vd = static_cast<Knot64 *>(ctx->pot_mem);
+    Knot64 *d_dd = d_vd + n_rec;
+    float4 *d_vf = reinterpret_cast<float4 *>(d_dd + n_rec);
+    float4 *d_df = d_vf + n_rec;
+    MG_CK(cudaMemcpy(d_vd, vd.data(), n_rec * sizeof(Knot64), cudaMemcpyHostToDevice));
+    MG_CK(cudaMemcpy(d_dd, dd.data(), n_rec * sizeof(Knot64), cudaMemcpyHostToDevice));
+    MG_CK(cudaMemcpy(d_vf, vf.data(), n_rec * sizeof(float4), cudaMemcpyHostToDevice));
+    MG_CK(cudaMemcpy(d_df, df.data(), n_rec * sizeof(float4), cudaMemcpyHostToDevice));
+
+    PotTables &pt = ctx->pt;
+    pt.nr = hp.nr;
+    pt.nrho = hp.nrho;
+    pt.inv_dr = hp.rho[0].inv_delta;
+    pt.inv_drho = hp.F[0].inv_delta;
+    pt.inv_dr_f = (float) pt.inv_dr;
+    pt.inv_drho_f = (float) pt.inv_drho;
+    pt.h_inv_dr_f = (float) (0.5 * ctx->g.a0 * pt.inv_dr);
+    int ele_of_type[3], pair_of_types[3][3];
+    ctx->types_ok_mask = 0;
+    for (int t = 0; t < 3; t++) {
+        int e = hp.ele(type_key(t));
+        if (e >= 0) ctx->types_ok_mask |= 1 << t;
+        if (e < 0) e = 0;
+        ele_of_type[t] = e;
+    }
+    for (int a = 0; a < 3; a++) {
+        const int ea = ele_of_type[a];
+        pt.F_v[a] = d_vd + base_F[ea]; pt.F_d[a] = d_dd + base_F[ea];
+        pt.rho_v[a] = d_vd + base_rho[ea]; pt.rho_d[a] = d_dd + base_rho[ea];
+        pt.F_vf[a] = d_vf + base_F[ea]; pt.F_df[a] = d_df + base_F[ea];
+        pt.rho_vf[a] = d_vf + base_rho[ea]; pt.rho_df_[a] = d_df + base_rho[ea];
+        for (int b = 0; b < 3; b++) {
+            const int q = HostPotential::pair_index(ea, ele_of_type[b]);
+            pair_of_types[a][b] = q;
+            pt.z_v[a][b] = d_vd + base_z[q]; pt.z_d[a][b] = d_dd + base_z[q];
+            pt.z_vf[a][b] = d_vf + base_z[q]; pt.z_df[a][b] = d_df + base_z[q];
+        }
+    }
+    set_type_maps(ele_of_type, pair_of_types, ctx->stream);
+    // the hit test uses rc = a0 * cutoff_radius_factor; the tables must reach it
+    if ((hp.nr - 1) * hp.dr + 1e-12 < ctx->g.rc) {
+        ctx->err = "potential r-table shorter than the cutoff radius";
+        return MG_ERR_POTENTIAL;
+    }
+    ctx->hp = hp;
+    ctx->pot_ready = true;
+    ctx->graph_dt = -1.0;  // rebuild graphs
+    return MG_OK;
+}
+
+mg_status check_types(mg_context *ctx, const mg_atom_element *atoms, int64_t n) {
+    for (int64_t i = 0; i < n; i++) {
+        const int t = atoms[i].type;
+        if (t < -1 || t > 2) { ctx->err = "atom type out of range"; return MG_ERR_ARG; }
+        if (t >= 0 && !(ctx->types_ok_mask & (1 << t))) { ctx->err = "potential has no element for an atom type present"; return MG_ERR_POTENTIAL; }
+    }
+    return MG_OK;
+}
+
+mg_status build_graph(mg_context *ctx) {
+    if (ctx->graph_exec && ctx->graph_dt == ctx->dt && ctx->graph_prec == ctx->precision) return MG_OK;
+    if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
+    cudaGraph_t graph;
+    MG_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    seq_step(ctx, nullptr);
+    MG_CK(cudaStreamEndCapture(ctx->stream, &graph));
+    size_t n_nodes = 0;
+    cudaGraphGetNodes(graph, nullptr, &n_nodes);
+    ctx->launches_per_step = static_cast<int>(n_nodes);
+    cudaError_t e = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { ctx->err = std::string("graph instantiate: ") + cudaGetErrorString(e); return MG_ERR_CUDA; }
+    ctx->graph_dt = ctx->dt;
+    ctx->graph_prec = ctx->precision;
+    return MG_OK;
+}
+
+mg_status read_device_errors(mg_context *ctx, uint32_t *bits) {
+    int cnt[CNT_WORDS];
+    MG_CK(cudaMemcpyAsync(cnt, ctx->in.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_CK(cudaStreamSynchronize(ctx->stream));
+    *bits = static_cast<uint32_t>(cnt[CNT_ERRORS]);
+    return MG_OK;
+}
+
+mg_status status_from_bits(mg_context *ctx, uint32_t bits) {
+    if (bits & MG_DEVERR_BAD_TYPE) { ctx->err = "atom type out of range or without a potential element"; return MG_ERR_ARG; }
+    if (bits & MG_DEVERR_OUT_OF_GRID) { ctx->err = "an index left the slot grid"; return MG_ERR_OUT_OF_GRID; }
+    if (bits & (MG_DEVERR_INTER_OVERFLOW | MG_DEVERR_GHOST_OVERFLOW | MG_DEVERR_DISPLACED_OVERFLOW)) {
+        ctx->err = "inter-atom list capacity exceeded";
+        return MG_ERR_CAPACITY;
+    }
+    return MG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mg_status mg_env_init(int32_t device) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { g_create_error = cudaGetErrorString(e); return MG_ERR_CUDA; }
+    return MG_OK;
+}
+mg_status mg_env_clean(void) { return MG_OK; }
+
+const char *mg_last_error(const mg_context *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+mg_status mg_create(const int64_t phase_space[3], double lattice_const, double rcf, int32_t precision,
+                    int64_t inter_capacity, mg_context **out) {
+    if (!out || !phase_space || !(lattice_const > 0) || !(rcf > 0)) { g_create_error = "bad argument"; return MG_ERR_ARG; }
+    if (precision != MG_PREC_FP64 && precision != MG_PREC_MIXED) { g_create_error = "bad precision"; return MG_ERR_ARG; }
+    *out = nullptr;
+    const int ghost = static_cast<int>(std::ceil(rcf)) + 1;       // src/simulation.cpp:120
+    const int cut_lattice = static_cast<int>(std::ceil(rcf));      // libcomm cut_lattice
+    for (int d = 0; d < 3; d++) {
+        if (phase_space[d] < 2 * ghost) { g_create_error = "every dimension needs at least 2*ghost unit cells"; return MG_ERR_ARG; }
+    }
+    const int64_t Sx = 2 * (phase_space[0] + 2 * ghost), Sy = phase_space[1] + 2 * ghost, Sz = phase_space[2] + 2 * ghost;
+    if (Sx * Sy * Sz >= (int64_t) 0x7fffffff - 1024) { g_create_error = "box too large for 32-bit slot indices"; return MG_ERR_ARG; }
+
+    auto *ctx = new mg_context();
+    ctx->precision = precision;
+    cudaGetDevice(&ctx->device);
+    Geom &g = ctx->g;
+    g.Sx = (int) Sx; g.Sy = (int) Sy; g.Sz = (int) Sz;
+    g.gx = 2 * ghost; g.gy = ghost; g.gz = ghost;
+    g.bx = (int) (2 * phase_space[0]); g.by = (int) phase_space[1]; g.bz = (int) phase_space[2];
+    g.n_slots = (int) (Sx * Sy * Sz);
+    g.n_local = g.bx * g.by * g.bz;
+    g.n_ghost_slots = g.n_slots - g.n_local;
+    for (int d = 0; d < 3; d++) g.cells[d] = (int) phase_space[d];
+    g.a0 = lattice_const;
+    g.rc = lattice_const * rcf;  // atom::atom, src/atom.cpp:14-19
+    g.rc2 = g.rc * g.rc;
+    g.thr = std::pow(0.2 * lattice_const, 2.0);
+    for (int d = 0; d < 3; d++) g.L[d] = phase_space[d] * lattice_const;
+    g.inv_h = 2.0 / lattice_const;
+    g.h_f = (float) (0.5 * lattice_const);
+    g.rc2_h = (float) (g.rc2 * g.inv_h * g.inv_h);
+
+    // offset tables, and the lattice gather order: pruned entries (site distance below
+    // rc + 0.4 a0, with margin) first, in reference order, then the rest
+    ctx->offs = make_offsets(Sx, Sy, cut_lattice, rcf);
+    ctx->n_full = static_cast<int>(ctx->offs.off[0].size());
+    if (ctx->n_full > kMaxFull || ctx->offs.off[1].size() != ctx->offs.off[0].size()) {
+        g_create_error = "offset table too large";
+        delete ctx;
+        return MG_ERR_ARG;
+    }
+    const double prune_r = rcf + 0.4 + 1e-6;
+    for (int p = 0; p < 2; p++) {
+        std::vector<int> near, rest;
+        for (int q = 0; q < ctx->n_full; q++) {
+            const double *v = &ctx->offs.vec[p][3 * q];
+            const double r = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            (r < prune_r ? near : rest).push_back(q);
+        }
+        if (p == 0) ctx->n_pruned = static_cast<int>(near.size());
+        ctx->lat_order[p] = near;
+        ctx->lat_order[p].insert(ctx->lat_order[p].end(), rest.begin(), rest.end());
+    }
+
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { g_create_error = cudaGetErrorString(e); delete ctx; return MG_ERR_CUDA; }
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+
+    auto fail = [&](cudaError_t err) {
+        g_create_error = std::string("device allocation: ") + cudaGetErrorString(err);
+        mg_destroy(ctx);
+        return MG_ERR_CUDA;
+    };
+    const size_t ns = static_cast<size_t>(g.n_slots);
+    Slots &s = ctx->s;
+    cudaError_t ae = cudaSuccess;
+#define ALLOC(p, n) do { if ((ae = dalloc(ctx, &(p), (n))) != cudaSuccess) return fail(ae); } while (0)
+    ALLOC(s.x, ns); ALLOC(s.y, ns); ALLOC(s.z, ns);
+    ALLOC(s.vx, ns); ALLOC(s.vy, ns); ALLOC(s.vz, ns);
+    ALLOC(s.fx, ns); ALLOC(s.fy, ns); ALLOC(s.fz, ns);
+    ALLOC(s.rho, ns); ALLOC(s.df, ns); ALLOC(s.e, ns);
+    ALLOC(s.type, ns); ALLOC(s.id, ns);
+    ALLOC(s.u4, ns); ALLOC(s.df32, ns);
+
+    Inter &in = ctx->in;
+    in.cap = static_cast<int>(inter_capacity > 0 ? inter_capacity : 16384);
+    in.gcap = 8 * in.cap;
+    in.dcap = next_pow2(in.cap);
+    in.fcap = in.cap;
+    const int nbuck = next_pow2(std::max(in.cap + in.gcap, in.dcap));
+    const size_t cap = in.cap, gcap = in.gcap;
+    ALLOC(in.cnt, CNT_WORDS);
+    ALLOC(in.id, cap); ALLOC(in.type, cap);
+    ALLOC(in.x, cap); ALLOC(in.y, cap); ALLOC(in.z, cap);
+    ALLOC(in.vx, cap); ALLOC(in.vy, cap); ALLOC(in.vz, cap);
+    ALLOC(in.fx, cap); ALLOC(in.fy, cap); ALLOC(in.fz, cap);
+    ALLOC(in.rho, cap); ALLOC(in.df, cap); ALLOC(in.e, cap);
+    ALLOC(in.gtype, gcap); ALLOC(in.groot, gcap);
+    ALLOC(in.gx, gcap); ALLOC(in.gy, gcap); ALLOC(in.gz, gcap); ALLOC(in.gdf, gcap);
+    ALLOC(in.scratch_i, 3 * cap); ALLOC(in.scratch_d, 13 * cap); ALLOC(in.scratch_u, cap);
+    ALLOC(in.displaced, (size_t) in.dcap);
+    ALLOC(in.claim, ns);
+    ALLOC(in.far_list, (size_t) in.fcap);
+    ALLOC(in.far_flag, ns);
+    ALLOC(in.bucket, (size_t) nbuck);
+    ALLOC(in.n_bucket, 1);
+    ctx->n_partials = ctx->num_sms * 4;
+    ALLOC(ctx->d_partials, (size_t) ctx->n_partials * 8);
+    ALLOC(ctx->d_thermo, 8);
+#undef ALLOC
+    e = cudaMemsetAsync(in.cnt, 0, CNT_WORDS * sizeof(int), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(in.claim, 0x7f, ns * sizeof(int), ctx->stream);  // 0x7f7f7f7f > any list index
+    if (e == cudaSuccess) e = cudaMemsetAsync(in.far_flag, 0, ns, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(in.n_bucket, 0, sizeof(int), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s.type, 0xff, ns, ctx->stream);  // all slots INVALID
+    if (e == cudaSuccess) e = cudaMemsetAsync(s.u4, 0xff, ns * sizeof(float4), ctx->stream);
+    if (e != cudaSuccess) return fail(e);
+    if (upload_tables(ctx) != MG_OK) { g_create_error = ctx->err; mg_destroy(ctx); return MG_ERR_CUDA; }
+    set_dt(ctx, 0.001);
+    *out = ctx;
+    return MG_OK;
+}
+
+mg_status mg_destroy(mg_context *ctx) {
+    if (!ctx) return MG_ERR_ARG;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    for (cudaEvent_t e : ctx->ev) cudaEventDestroy(e);
+    for (void *p : ctx->dev_allocs) cudaFree(p);
+    if (ctx->pot_mem) cudaFree(ctx->pot_mem);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return MG_OK;
+}
+
+mg_status mg_grid(const mg_context *ctx, int64_t out[6]) {
+    if (!ctx || !out) return MG_ERR_ARG;
+    out[0] = ctx->g.Sx; out[1] = ctx->g.Sy; out[2] = ctx->g.Sz;
+    out[3] = ctx->g.gx; out[4] = ctx->g.gy; out[5] = ctx->g.gz;
+    return MG_OK;
+}
+
+mg_status mg_set_precision(mg_context *ctx, int32_t precision) {
+    if (!ctx || (precision != MG_PREC_FP64 && precision != MG_PREC_MIXED)) return MG_ERR_ARG;
+    ctx->precision = precision;
+    ctx->prepared = false;  // derived arrays (u4, df32) must be rebuilt by an upload
+    return MG_OK;
+}
+
+mg_status mg_nei_offset_init(mg_context *ctx, const int64_t *full_even, const int64_t *full_odd, int32_t n_full,
+                             const int64_t *half_even, const int64_t *half_odd, int32_t n_half) {
+    if (!ctx || !full_even || !full_odd || !half_even || !half_odd) return MG_ERR_ARG;
+    if (n_full != ctx->n_full || n_half != (int32_t) ctx->offs.half[0].size()) {
+        ctx->err = "offset tables differ in length";
+        return MG_ERR_ARG;
+    }
+    for (int i = 0; i < n_full; i++)
+        if (full_even[i] != ctx->offs.off[0][i] || full_odd[i] != ctx->offs.off[1][i]) { ctx->err = "full offset tables differ"; return MG_ERR_ARG; }
+    for (int i = 0; i < n_half; i++)
+        if (half_even[i] != ctx->offs.half[0][i] || half_odd[i] != ctx->offs.half[1][i]) { ctx->err = "half offset tables differ"; return MG_ERR_ARG; }
+    return MG_OK;
+}
+
+mg_status mg_nei_offsets(const mg_context *ctx, int32_t which, int64_t *out, int32_t cap, int32_t *n) {
+    if (!ctx || !n || which < 0 || which > 5) return MG_ERR_ARG;
+    std::vector<int64_t> v;
+    if (which <= 1) v = ctx->offs.off[which];
+    else if (which <= 3) v = ctx->offs.half[which - 2];
+    else {
+        const int p = which - 4;
+        for (int q = 0; q < ctx->n_pruned; q++) v.push_back(ctx->offs.off[p][ctx->lat_order[p][q]]);
+    }
+    *n = static_cast<int32_t>(v.size());
+    for (int32_t i = 0; i < *n && i < cap && out; i++) out[i] = v[i];
+    return MG_OK;
+}
+
+mg_status mg_pot_init_setfl(mg_context *ctx, const char *path) {
+    if (!ctx || !path) return MG_ERR_ARG;
+    HostPotential hp;
+    if (!read_setfl(path, hp, ctx->err)) return MG_ERR_POTENTIAL;
+    return install_potential(ctx, hp);
+}
+
+mg_status mg_pot_init_tables(mg_context *ctx, int32_t n_ele, const int32_t *zs, int32_t nrho, double drho, int32_t nr,
+                             double dr, double cutoff, const double *F, const double *rho, const double *rphi) {
+    if (!ctx || !zs || !F || !rho || !rphi) return MG_ERR_ARG;
+    HostPotential hp;
+    if (!build_potential(n_ele, zs, nrho, drho, nr, dr, cutoff, F, rho, rphi, hp, ctx->err)) return MG_ERR_POTENTIAL;
+    return install_potential(ctx, hp);
+}
+
+mg_status mg_pot_spline(const mg_context *ctx, int32_t kind, int32_t e1, int32_t e2, double *out, int32_t cap,
+                        int32_t *n) {
+    if (!ctx || !n || kind < 0 || kind > 2) return MG_ERR_ARG;
+    if (!ctx->pot_ready) return MG_ERR_POTENTIAL;
+    const HostPotential &p = ctx->hp;
+    if (e1 < 0 || e1 >= p.n_ele || e2 < 0 || e2 >= p.n_ele) return MG_ERR_ARG;
+    const HostSpline &sp = kind == 0 ? p.F[e1] : kind == 1 ? p.rho[e1] : p.z2[HostPotential::pair_index(e1, e2)];
+    *n = sp.n;
+    for (int m = 0; m < sp.n && out && 7 * m + 6 < cap; m++) {
+        out[7 * m + 0] = sp.c0[m]; out[7 * m + 1] = sp.c1[m]; out[7 * m + 2] = sp.c2[m]; out[7 * m + 3] = sp.c3[m];
+        out[7 * m + 4] = sp.d0[m]; out[7 * m + 5] = sp.d1[m]; out[7 * m + 6] = sp.d2[m];
+    }
+    return MG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// hooks (src/arch/arch_imp.h:27-31)
+// ---------------------------------------------------------------------------------------------
+static mg_status hook_upload(mg_context *ctx, mg_atom_element *atoms, double cutoff) {
+    if (!ctx || !atoms) return MG_ERR_ARG;
+    mg_status st = require_ready(ctx);
+    if (st != MG_OK) return st;
+    if (std::fabs(cutoff - ctx->g.rc) > 1e-12 * ctx->g.rc) { ctx->err = "cutoff radius differs from the context's"; return MG_ERR_ARG; }
+    if ((st = ensure_aos(ctx)) != MG_OK) return st;
+    MG_CK(cudaMemcpyAsync(ctx->d_aos, atoms, sizeof(mg_atom_element) * ctx->g.n_slots, cudaMemcpyHostToDevice, ctx->stream));
+    launch_unpack_aos(ctx->lc(), ctx->g, ctx->d_aos, ctx->s, ctx->in, ctx->types_ok_mask, ctx->mixed());
+    launch_far_rebuild(ctx->lc(), ctx->g, ctx->s, ctx->in);
+    return check_launch(ctx);
+}
+static mg_status hook_download(mg_context *ctx, mg_atom_element *atoms, int fields) {
+    launch_pack_aos(ctx->lc(), ctx->g, ctx->d_aos, ctx->s, fields, ctx->mixed());
+    mg_status st = check_launch(ctx);
+    if (st != MG_OK) return st;
+    MG_CK(cudaMemcpyAsync(atoms, ctx->d_aos, sizeof(mg_atom_element) * ctx->g.n_slots, cudaMemcpyDeviceToHost, ctx->stream));
+    uint32_t bits = 0;
+    if ((st = read_device_errors(ctx, &bits)) != MG_OK) return st;
+    return status_from_bits(ctx, bits);
+}
+
+mg_status mg_eam_rho_calc(mg_context *ctx, mg_atom_element *atoms, double cutoff_radius) {
+    mg_status st = hook_upload(ctx, atoms, cutoff_radius);
+    if (st != MG_OK) return st;
+    launch_lat_rho(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, ctx->mixed(), true);
+    launch_far_scatter(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, 0, ctx->mixed());
+    return hook_download(ctx, atoms, PACK_RHO);
+}
+mg_status mg_eam_df_calc(mg_context *ctx, mg_atom_element *atoms, double cutoff_radius) {
+    mg_status st = hook_upload(ctx, atoms, cutoff_radius);
+    if (st != MG_OK) return st;
+    launch_lat_df(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, ctx->mixed(), true);
+    return hook_download(ctx, atoms, PACK_DF);
+}
+mg_status mg_eam_force_calc(mg_context *ctx, mg_atom_element *atoms, double cutoff_radius) {
+    mg_status st = hook_upload(ctx, atoms, cutoff_radius);
+    if (st != MG_OK) return st;
+    StepParams none{};
+    launch_lat_force(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, none, false, ctx->mixed(), true);
+    launch_far_scatter(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, 1, ctx->mixed());
+    return hook_download(ctx, atoms, PACK_F);
+}
+
+// ---------------------------------------------------------------------------------------------
+// resident state
+// ---------------------------------------------------------------------------------------------
+mg_status mg_upload(mg_context *ctx, const mg_atom_element *atoms, int64_t n_slots, const mg_atom_element *inter,
+                    int64_t n_inter) {
+    if (!ctx || !atoms || n_slots != ctx->g.n_slots || n_inter < 0 || (n_inter > 0 && !inter)) return MG_ERR_ARG;
+    mg_status st = require_ready(ctx);
+    if (st != MG_OK) return st;
+    if (n_inter > ctx->in.cap) { ctx->err = "inter list larger than the context capacity"; return MG_ERR_CAPACITY; }
+    if ((st = check_types(ctx, inter, n_inter)) != MG_OK) return st;
+    if ((st = ensure_aos(ctx)) != MG_OK) return st;
+    MG_CK(cudaMemcpyAsync(ctx->d_aos, atoms, sizeof(mg_atom_element) * n_slots, cudaMemcpyHostToDevice, ctx->stream));
+    launch_unpack_aos(ctx->lc(), ctx->g, ctx->d_aos, ctx->s, ctx->in, ctx->types_ok_mask, ctx->mixed());
+    // inter list: records -> SoA columns via host staging
+    std::vector<uint64_t> id(n_inter);
+    std::vector<int> ty(n_inter);
+    std::vector<double> col(13 * (size_t) n_inter);
+    for (int64_t a = 0; a < n_inter; a++) {
+        const mg_atom_element &r = inter[a];
+        id[a] = r.id; ty[a] = r.type;
+        const double v[11] = {r.x[0], r.x[1], r.x[2], r.v[0], r.v[1], r.v[2], r.f[0], r.f[1], r.f[2], r.rho, r.df};
+        for (int k = 0; k < 11; k++) col[k * n_inter + a] = v[k];
+    }
+    Inter &in = ctx->in;
+    double *dst[11] = {in.x, in.y, in.z, in.vx, in.vy, in.vz, in.fx, in.fy, in.fz, in.rho, in.df};
+    if (n_inter > 0) {
+        MG_CK(cudaMemcpyAsync(in.id, id.data(), n_inter * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
+        MG_CK(cudaMemcpyAsync(in.type, ty.data(), n_inter * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+        for (int k = 0; k < 11; k++)
+            MG_CK(cudaMemcpyAsync(dst[k], col.data() + k * n_inter, n_inter * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    // the ghost list and the displaced list restart empty; the far list is rebuilt from positions
+    launch_set_counts(ctx->lc(), ctx->in, static_cast<int>(n_inter));
+    launch_far_rebuild(ctx->lc(), ctx->g, ctx->s, ctx->in);
+    ctx->prepared = false;
+    ctx->energy_valid = false;
+    return check_launch(ctx);
+}
+
+mg_status mg_download(mg_context *ctx, mg_atom_element *atoms, int64_t n_slots, mg_atom_element *inter,
+                      int64_t inter_cap, int64_t *n_inter) {
+    if (!ctx || !atoms || n_slots != ctx->g.n_slots) return MG_ERR_ARG;
+    mg_status st = ensure_aos(ctx);
+    if (st != MG_OK) return st;
+    launch_pack_aos(ctx->lc(), ctx->g, ctx->d_aos, ctx->s, PACK_ALL, ctx->mixed());
+    if ((st = check_launch(ctx)) != MG_OK) return st;
+    MG_CK(cudaMemcpyAsync(atoms, ctx->d_aos, sizeof(mg_atom_element) * n_slots, cudaMemcpyDeviceToHost, ctx->stream));
+    int cnt[CNT_WORDS];
+    MG_CK(cudaMemcpyAsync(cnt, ctx->in.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_CK(cudaStreamSynchronize(ctx->stream));
+    const int64_t n = cnt[CNT_INTER];
+    if (n_inter) *n_inter = n;
+    const int64_t m = std::min<int64_t>(n, inter ? inter_cap : 0);
+    if (m > 0) {
+        Inter &in = ctx->in;
+        std::vector<uint64_t> id(m);
+        std::vector<int> ty(m);
+        std::vector<double> col(11 * (size_t) m);
+        const double *src[11] = {in.x, in.y, in.z, in.vx, in.vy, in.vz, in.fx, in.fy, in.fz, in.rho, in.df};
+        MG_CK(cudaMemcpyAsync(id.data(), in.id, m * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream));
+        MG_CK(cudaMemcpyAsync(ty.data(), in.type, m * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        for (int k = 0; k < 11; k++)
+            MG_CK(cudaMemcpyAsync(col.data() + k * m, src[k], m * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        MG_CK(cudaStreamSynchronize(ctx->stream));
+        for (int64_t a = 0; a < m; a++) {
+            mg_atom_element &r = inter[a];
+            std::memset(&r, 0, sizeof(r));
+            r.id = id[a]; r.type = ty[a];
+            r.x[0] = col[0 * m + a]; r.x[1] = col[1 * m + a]; r.x[2] = col[2 * m + a];
+            r.v[0] = col[3 * m + a]; r.v[1] = col[4 * m + a]; r.v[2] = col[5 * m + a];
+            r.f[0] = col[6 * m + a]; r.f[1] = col[7 * m + a]; r.f[2] = col[8 * m + a];
+            r.rho = col[9 * m + a]; r.df = col[10 * m + a];
+        }
+    }
+    return MG_OK;
+}
+
+mg_status mg_download_ghost_inter(mg_context *ctx, mg_atom_element *ghost, int64_t cap, int64_t *n_ghost) {
+    if (!ctx) return MG_ERR_ARG;
+    int cnt[CNT_WORDS];
+    MG_CK(cudaMemcpyAsync(cnt, ctx->in.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_CK(cudaStreamSynchronize(ctx->stream));
+    const int64_t n = cnt[CNT_GHOST];
+    if (n_ghost) *n_ghost = n;
+    const int64_t m = std::min<int64_t>(n, ghost ? cap : 0);
+    if (m > 0) {
+        Inter &in = ctx->in;
+        std::vector<int> ty(m);
+        std::vector<double> col(4 * (size_t) m);
+        const double *src[4] = {in.gx, in.gy, in.gz, in.gdf};
+        MG_CK(cudaMemcpyAsync(ty.data(), in.gtype, m * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        for (int k = 0; k < 4; k++)
+            MG_CK(cudaMemcpyAsync(col.data() + k * m, src[k], m * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        MG_CK(cudaStreamSynchronize(ctx->stream));
+        for (int64_t a = 0; a < m; a++) {
+            mg_atom_element &r = ghost[a];
+            std::memset(&r, 0, sizeof(r));
+            r.type = ty[a];
+            r.x[0] = col[a]; r.x[1] = col[m + a]; r.x[2] = col[2 * m + a];
+            r.df = col[3 * m + a];
+        }
+    }
+    return MG_OK;
+}
+
+mg_status mg_set_timestep(mg_context *ctx, double dt) {
+    if (!ctx || !(dt > 0)) return MG_ERR_ARG;
+    set_dt(ctx, dt);
+    return MG_OK;
+}
+
+mg_status mg_prepare(mg_context *ctx) {
+    if (!ctx) return MG_ERR_ARG;
+    mg_status st = require_ready(ctx);
+    if (st != MG_OK) return st;
+    // exchangeAtomFirst, clearForce, computeEam (src/simulation.cpp:209-219); the lattice passes assign
+    // instead of accumulate, which is what clearForce + accumulate gives
+    seq_compute_eam(ctx, false, false, 0, nullptr);
+    if ((st = check_launch(ctx)) != MG_OK) return st;
+    uint32_t bits = 0;
+    if ((st = read_device_errors(ctx, &bits)) != MG_OK) return st;
+    ctx->prepared = true;
+    return status_from_bits(ctx, bits);
+}
+
+mg_status mg_simulate(mg_context *ctx, int64_t nsteps, int32_t sync) {
+    if (!ctx || nsteps < 0) return MG_ERR_ARG;
+    if (!ctx->prepared) { ctx->err = "mg_prepare must run before mg_simulate"; return MG_ERR_STATE; }
+    mg_status st;
+    if (ctx->timing) {
+        const size_t need = static_cast<size_t>(nsteps) * (kNumTimers + 1);
+        while (ctx->ev.size() < need) {
+            cudaEvent_t e;
+            MG_CK(cudaEventCreate(&e));
+            ctx->ev.push_back(e);
+        }
+        for (int64_t i = 0; i < nsteps; i++) {
+            Timer t{ctx, i};
+            seq_step(ctx, &t);
+        }
+        if ((st = check_launch(ctx)) != MG_OK) return st;
+        MG_CK(cudaStreamSynchronize(ctx->stream));
+        ctx->timer_ms.assign(kNumTimers, 0.0);
+        for (int64_t i = 0; i < nsteps; i++) {
+            for (int k = 0; k < kNumTimers - 1; k++) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, ctx->ev[i * (kNumTimers + 1) + k], ctx->ev[i * (kNumTimers + 1) + k + 1]);
+                ctx->timer_ms[k] += ms;
+            }
+        }
+        ctx->timed_steps = nsteps;
+    } else {
+        if ((st = build_graph(ctx)) != MG_OK) return st;
+        for (int64_t i = 0; i < nsteps; i++) MG_CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    }
+    ctx->energy_valid = false;
+    if (sync) {
+        uint32_t bits = 0;
+        if ((st = read_device_errors(ctx, &bits)) != MG_OK) return st;
+        return status_from_bits(ctx, bits);
+    }
+    return MG_OK;
+}
+
+mg_status mg_phase(mg_context *ctx, int32_t phase) {
+    if (!ctx || phase < 0 || phase > 6) return MG_ERR_ARG;
+    mg_status st = require_ready(ctx);
+    if (st != MG_OK) return st;
+    const LaunchCtx lc = ctx->lc();
+    switch (phase) {
+        case 0: seq_firststep(ctx, false, nullptr); break;
+        case 1:
+            launch_decide_scan(lc, ctx->g, ctx->s, ctx->in);
+            launch_inter_manage(lc, ctx->g, ctx->s, ctx->in, MANAGE_DECIDE | MANAGE_CLEAR_GHOST, ctx->mixed());
+            break;
+        case 2: launch_inter_manage(lc, ctx->g, ctx->s, ctx->in, MANAGE_EXCHANGE, ctx->mixed()); break;
+        case 3: launch_inter_manage(lc, ctx->g, ctx->s, ctx->in, MANAGE_BORDER, ctx->mixed()); break;
+        case 4: launch_ghost_copy(lc, ctx->g, ctx->s, ctx->mixed()); break;
+        case 5: seq_compute_eam(ctx, false, false, 0, nullptr); break;
+        case 6: launch_secondstep(lc, ctx->g, ctx->s, ctx->in, ctx->sp, true); break;
+    }
+    if ((st = check_launch(ctx)) != MG_OK) return st;
+    uint32_t bits = 0;
+    if ((st = read_device_errors(ctx, &bits)) != MG_OK) return st;
+    ctx->energy_valid = false;
+    return status_from_bits(ctx, bits);
+}
+
+mg_status mg_collision_step(mg_context *ctx, const int32_t lat[4], const double dir[3], double energy) {
+    if (!ctx || !lat || !dir) return MG_ERR_ARG;
+    mg_status st = require_ready(ctx);
+    if (st != MG_OK) return st;
+    // atom::setv bounds (src/atom.cpp:477-482), one rank: the sub-box starts at 0
+    const Geom &g = ctx->g;
+    if (lat[3] < 0 || lat[3] > 1) { ctx->err = "PKA basis index must be 0 or 1"; return MG_ERR_ARG; }
+    if ((lat[0] * 2) >= 0 && (lat[0] * 2) < g.bx && lat[1] >= 0 && lat[1] < g.by && lat[2] >= 0 && lat[2] < g.bz) {
+        const int64_t kk = ((int64_t) (lat[2] + g.gz) * g.Sy + (lat[1] + g.gy)) * g.Sx + (lat[0] * 2 + g.gx) + lat[3];
+        if (kk < 0 || kk >= g.n_slots) { ctx->err = "PKA slot outside the grid"; return MG_ERR_ARG; }
+        launch_setv(ctx->lc(), g, ctx->s, kk, dir, energy);
+    }
+    // exchangeInter, borderInter (the ghost list is not cleared here, as in the reference),
+    // exchangeAtom, clearForce, computeEam (src/simulation.cpp:282-291)
+    launch_inter_manage(ctx->lc(), g, ctx->s, ctx->in, MANAGE_EXCHANGE | MANAGE_BORDER, ctx->mixed());
+    seq_compute_eam(ctx, false, false, 0, nullptr);
+    if ((st = check_launch(ctx)) != MG_OK) return st;
+    uint32_t bits = 0;
+    if ((st = read_device_errors(ctx, &bits)) != MG_OK) return st;
+    ctx->energy_valid = false;
+    return status_from_bits(ctx, bits);
+}
+
+mg_status mg_rescale(mg_context *ctx, double t_set, uint64_t n_atoms) {
+    if (!ctx || n_atoms < 2) return MG_ERR_ARG;
+    launch_thermo(ctx->lc(), ctx->g, ctx->s, ctx->in, false, ctx->d_partials, ctx->n_partials, ctx->d_thermo);
+    launch_rescale(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->d_thermo, t_set, n_atoms);
+    mg_status st = check_launch(ctx);
+    if (st != MG_OK) return st;
+    MG_CK(cudaStreamSynchronize(ctx->stream));
+    return MG_OK;
+}
+
+mg_status mg_thermo(mg_context *ctx, int32_t with_energy, mg_thermo_out *out) {
+    if (!ctx || !out) return MG_ERR_ARG;
+    mg_status st;
+    if (with_energy) {
+        if ((st = require_ready(ctx)) != MG_OK) return st;
+        launch_energy(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, ctx->mixed());
+        launch_far_scatter(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, 2, ctx->mixed());
+        launch_inter_energy(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, ctx->mixed());
+        ctx->energy_valid = true;
+    }
+    launch_thermo(ctx->lc(), ctx->g, ctx->s, ctx->in, with_energy != 0, ctx->d_partials, ctx->n_partials, ctx->d_thermo);
+    if ((st = check_launch(ctx)) != MG_OK) return st;
+    double h[6];
+    int cnt[CNT_WORDS];
+    MG_CK(cudaMemcpyAsync(h, ctx->d_thermo, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_CK(cudaMemcpyAsync(cnt, ctx->in.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_CK(cudaStreamSynchronize(ctx->stream));
+    std::memset(out, 0, sizeof(*out));
+    out->mvv = h[0];
+    out->kinetic_energy = h[0] / 2;
+    out->force_sum[0] = h[1]; out->force_sum[1] = h[2]; out->force_sum[2] = h[3];
+    out->potential_energy = with_energy ? h[4] : 0.0;
+    out->n_vacancy = static_cast<int64_t>(h[5]);
+    out->n_inter = cnt[CNT_INTER];
+    out->n_ghost_inter = cnt[CNT_GHOST];
+    out->device_errors = static_cast<uint32_t>(cnt[CNT_ERRORS]);
+    return MG_OK;
+}
+
+mg_status mg_download_energies(mg_context *ctx, double *per_slot, int64_t n_slots, double *per_inter,
+                               int64_t inter_cap) {
+    if (!ctx || !per_slot || n_slots != ctx->g.n_slots) return MG_ERR_ARG;
+    if (!ctx->energy_valid) { ctx->err = "no energy pass since the last state change"; return MG_ERR_STATE; }
+    MG_CK(cudaMemcpyAsync(per_slot, ctx->s.e, n_slots * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    int cnt[CNT_WORDS];
+    MG_CK(cudaMemcpyAsync(cnt, ctx->in.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_CK(cudaStreamSynchronize(ctx->stream));
+    // local slots only: ghosts and vacancies are reported as 0
+    std::vector<int8_t> ty(n_slots);
+    MG_CK(cudaMemcpy(ty.data(), ctx->s.type, n_slots, cudaMemcpyDeviceToHost));
+    const Geom &g = ctx->g;
+    for (int64_t s = 0; s < n_slots; s++) {
+        const int64_t X = s % g.Sx, r = s / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
+        const bool local = X >= g.gx && X < g.gx + g.bx && Y >= g.gy && Y < g.gy + g.by && Z >= g.gz && Z < g.gz + g.bz;
+        if (!local || ty[s] < 0) per_slot[s] = 0.0;
+    }
+    const int64_t m = std::min<int64_t>(cnt[CNT_INTER], per_inter ? inter_cap : 0);
+    if (m > 0) MG_CK(cudaMemcpy(per_inter, ctx->in.e, m * sizeof(double), cudaMemcpyDeviceToHost));
+    return MG_OK;
+}
+
+mg_status mg_clear_errors(mg_context *ctx) {
+    if (!ctx) return MG_ERR_ARG;
+    int z = 0;
+    MG_CK(cudaMemcpyAsync(ctx->in.cnt + CNT_ERRORS, &z, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    MG_CK(cudaStreamSynchronize(ctx->stream));
+    return MG_OK;
+}
+
+mg_status mg_step_host(mg_context *ctx, mg_atom_element *atoms, int64_t n_slots, mg_atom_element *inter,
+                       int64_t inter_cap, int64_t *n_inter, int64_t nsteps) {
+    if (!ctx || !atoms || !n_inter) return MG_ERR_ARG;
+    mg_status st = mg_upload(ctx, atoms, n_slots, inter, std::min<int64_t>(*n_inter, inter_cap));
+    if (st != MG_OK) return st;
+    ctx->prepared = true;  // the host state carries forces from its previous computeEam
+    if ((st = mg_simulate(ctx, nsteps, 0)) != MG_OK) return st;
+    return mg_download(ctx, atoms, n_slots, inter, inter_cap, n_inter);
+}
+
+mg_status mg_ws_map(mg_context *ctx, const double *xyz, int64_t n, int64_t *coords, uint32_t *flags, int64_t *index) {
+    if (!ctx || !xyz || !coords || !flags || !index || n < 0) return MG_ERR_ARG;
+    if (n == 0) return MG_OK;
+    if (n > ctx->ws_cap) {
+        MG_CK(dalloc(ctx, &ctx->d_ws_xyz, 3 * (size_t) n));
+        MG_CK(dalloc(ctx, &ctx->d_ws_coords, 3 * (size_t) n));
+        MG_CK(dalloc(ctx, &ctx->d_ws_flags, (size_t) n));
+        MG_CK(dalloc(ctx, &ctx->d_ws_index, (size_t) n));
+        ctx->ws_cap = n;
+    }
+    MG_CK(cudaMemcpyAsync(ctx->d_ws_xyz, xyz, 3 * n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    launch_ws_map(ctx->lc(), ctx->g, ctx->d_ws_xyz, n, ctx->d_ws_coords, ctx->d_ws_flags, ctx->d_ws_index);
+    mg_status st = check_launch(ctx);
+    if (st != MG_OK) return st;
+    MG_CK(cudaMemcpyAsync(coords, ctx->d_ws_coords, 3 * n * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_CK(cudaMemcpyAsync(flags, ctx->d_ws_flags, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_CK(cudaMemcpyAsync(index, ctx->d_ws_index, n * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_CK(cudaStreamSynchronize(ctx->stream));
+    return MG_OK;
+}
+
+mg_status mg_enable_timing(mg_context *ctx, int32_t on) {
+    if (!ctx) return MG_ERR_ARG;
+    ctx->timing = on != 0;
+    return MG_OK;
+}
+
+mg_status mg_kernel_times(const mg_context *ctx, double *ms, int32_t cap, int32_t *n, const char **names) {
+    if (!ctx || !n) return MG_ERR_ARG;
+    *n = kNumTimers - 1;
+    for (int k = 0; k < kNumTimers - 1 && k < cap; k++) {
+        if (ms) ms[k] = ctx->timed_steps ? ctx->timer_ms.size() > (size_t) k ? ctx->timer_ms[k] / ctx->timed_steps : 0.0 : 0.0;
+        if (names) names[k] = kTimerNames[k];
+    }
+    return MG_OK;
+}
+
+mg_status mg_launches_per_step(const mg_context *ctx, int32_t *n) {
+    if (!ctx || !n) return MG_ERR_ARG;
+    *n = ctx->launches_per_step > 0 ? ctx->launches_per_step : kLaunchesPerStep;
+    return MG_OK;
+}
+
+void *mg_stream(const mg_context *ctx) { return ctx ? (void *) ctx->stream : nullptr; }
+
+mg_status mg_host_register(void *ptr, uint64_t bytes) {
+    if (!ptr || bytes == 0) return MG_ERR_ARG;
+    cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+    if (e != cudaSuccess) { g_create_error = cudaGetErrorString(e); return MG_ERR_CUDA; }
+    return MG_OK;
+}
+mg_status mg_host_unregister(void *ptr) {
+    if (!ptr) return MG_ERR_ARG;
+    cudaError_t e = cudaHostUnregister(ptr);
+    if (e != cudaSuccess) { g_create_error = cudaGetErrorString(e); return MG_ERR_CUDA; }
+    return MG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,210 @@
+// Internal declarations shared by the misa_gb300 translation units (host + device).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/misa_gb300.h"
+
+namespace mg {
+
+constexpr int kInvalid = -1;                 // atom_type::INVALID (src/types/atom_types.h:27)
+constexpr double kBoltz = 8.617343e-5;       // src/types/pre_define.h:11
+constexpr double kMvv2e = 1.0364269e-4;      // src/types/pre_define.h:18
+constexpr double kFtm2v = (1.0 / kMvv2e);    // src/types/pre_define.h:19
+constexpr double kNeiLatCutoff = 0.5;        // src/md_building_config.h.in:24
+constexpr int kMaxFull = 256;                // capacity of a full offset table per parity
+constexpr int kMaxPruned = 128;              // capacity of a pruned full table per parity
+
+// box flags (src/lattice/box.h:12-20)
+constexpr uint32_t kInBox = 0, kXLow = 1u, kXHigh = 2u, kYLow = 4u, kYHigh = 8u, kZLow = 16u, kZHigh = 32u;
+
+// device counters / flags word indices
+enum { CNT_INTER = 0, CNT_GHOST = 1, CNT_DISPLACED = 2, CNT_ERRORS = 3, CNT_FAR = 4, CNT_WORDS = 8 };
+
+inline double atom_mass(int type) {  // src/types/atom_types.h:42-53
+    switch (type) {
+        case 0: return 55.845;
+        case 1: return 63.546;
+        case 2: return 58.6934;
+        default: return 0;
+    }
+}
+inline int type_key(int type) {  // src/types/atom_types.h:61-73
+    switch (type) {
+        case 0: return 26;
+        case 1: return 29;
+        case 2: return 28;
+        default: return 0;
+    }
+}
+
+// Slot grid of one rank owning the whole periodic box. x is doubled (even = cube corner,
+// odd = body centre); linear index (z * Sy + y) * Sx + x.
+struct Geom {
+    int Sx, Sy, Sz;          // ghost-extended slot grid
+    int gx, gy, gz;          // ghost widths (gx doubled)
+    int bx, by, bz;          // box sizes (bx doubled)
+    int n_slots, n_local, n_ghost_slots;
+    int cells[3];            // phase space in unit cells
+    double a0;               // lattice constant (Angstrom)
+    double rc, rc2;          // cutoff radius and its square
+    double thr;              // pow(0.2 a0, 2): displacement threshold of atom::decide
+    double L[3];             // periodic lengths
+    double inv_h;            // 2 / a0: inverse of the half lattice constant
+    float h_f;               // a0 / 2 (float)
+    float rc2_h;             // (rc / h)^2 in half-lattice units
+};
+
+// Lattice slot arrays (structure of arrays over every slot, ghosts included).
+struct Slots {
+    double *x, *y, *z;
+    double *vx, *vy, *vz;
+    double *fx, *fy, *fz;
+    double *rho, *df;
+    double *e;               // per-atom energy (energy pass only)
+    int8_t *type;
+    uint64_t *id;
+    float4 *u4;              // mixed form: displacement from the site in half-lattice units, w = type bits
+    float *df32;             // mixed form: F'(rho) in float
+};
+
+// Inter-atom lists (local list in list order; ghost list in receive order).
+struct Inter {
+    int cap, gcap;
+    int *cnt;                // CNT_* words
+    uint64_t *id;
+    int *type;
+    double *x, *y, *z, *vx, *vy, *vz, *fx, *fy, *fz, *rho, *df, *e;
+    // ghost inter atoms
+    int *gtype, *groot;      // groot: index of the local inter atom this ghost is an image of
+    double *gx, *gy, *gz, *gdf;
+    // scratch for compaction / sorting (size cap + gcap)
+    int *scratch_i;          // 2 * (cap + gcap)
+    double *scratch_d;       // 13 * cap
+    uint64_t *scratch_u;     // cap
+    // displaced lattice slots found by the decide scan (unordered)
+    int *displaced;
+    int dcap;
+    // per-slot claim word for recombination (INT_MAX when free)
+    int *claim;
+    // lattice atoms farther than 0.2 a0 from their site (only recombined atoms after decide):
+    // they gather over the whole offset table and scatter the pairs the pruned gathers miss
+    int *far_list;
+    int8_t *far_flag;        // per slot, 1 for members of far_list
+    int fcap;
+    // buckets: sorted (key, ref) pairs; ref < cap: local index, else cap + ghost index
+    long long *bucket;       // (key << 32) | ref packed, sorted ascending
+    int *n_bucket;
+};
+
+// One FP64 spline knot record (32 bytes, read as two 16-byte loads).
+struct alignas(32) Knot64 {
+    double a, b, c, d;
+};
+
+// Spline tables on the device. Value records {c0,c1,c2,c3}; derivative records {d0,d1,d2,0}.
+struct PotTables {
+    int nr, nrho;
+    double inv_dr, inv_drho;
+    float inv_dr_f, inv_drho_f, h_inv_dr_f;   // h_inv_dr_f = (a0/2) / dr
+    // per atom type (0..2): pointers into the element tables
+    const Knot64 *rho_v[3], *rho_d[3], *F_v[3], *F_d[3];
+    const Knot64 *z_v[3][3], *z_d[3][3];
+    const float4 *rho_vf[3], *rho_df_[3], *F_vf[3], *F_df[3];
+    const float4 *z_vf[3][3], *z_df[3][3];
+};
+
+// Constant per-step parameters.
+struct StepParams {
+    double dt;
+    double dt_inv_m[3];
+};
+
+// Host-side spline (FP64 coefficients), built identically to the setfl interpolation scheme.
+struct HostSpline {
+    int n = 0;
+    double delta = 0, inv_delta = 0;
+    std::vector<double> c0, c1, c2, c3, d0, d1, d2;
+    void build(const std::vector<double> &f, double dlt);
+};
+
+struct HostPotential {
+    int n_ele = 0;
+    std::vector<int> z;
+    int nrho = 0, nr = 0;
+    double drho = 0, dr = 0, cutoff = 0;
+    std::vector<HostSpline> F, rho, z2;   // z2 lower-triangle pair order
+    static int pair_index(int a, int b) {
+        if (a < b) { int t = a; a = b; b = t; }
+        return a * (a + 1) / 2 + b;
+    }
+    int ele(int key) const {
+        for (int i = 0; i < n_ele; i++) if (z[i] == key) return i;
+        return -1;
+    }
+};
+
+bool read_setfl(const std::string &path, HostPotential &p, std::string &err);
+bool build_potential(int n_ele, const int32_t *zs, int nrho, double drho, int nr, double dr, double cutoff,
+                     const double *F, const double *rho, const double *rphi, HostPotential &p, std::string &err);
+
+// Offset tables (restatement of NeighbourIndex::make, src/atom/neighbour_index.inl:13-76) plus the
+// real-space site vector (in units of a0) of every entry.
+struct OffsetTable {
+    std::vector<int64_t> off[2];          // full table per parity (0 even, 1 odd)
+    std::vector<int64_t> half[2];
+    std::vector<double> vec[2];           // 3 doubles per full entry
+};
+OffsetTable make_offsets(int64_t size_x, int64_t size_y, int cut_lattice, double rcf);
+
+// ---- kernel launchers (defined in the .cu files) ----
+struct LaunchCtx {
+    cudaStream_t stream;
+    int num_sms;
+};
+
+void set_constant_tables(const int *full_even, const int *full_odd, int n_full, const int *pruned_even,
+                         const int *pruned_odd, int n_pruned, const float *dsite_even, const float *dsite_odd,
+                         cudaStream_t stream);
+
+void launch_unpack_aos(const LaunchCtx &lc, const Geom &g, const mg_atom_element *aos, Slots s, Inter in, int types_ok_mask,
+                       bool mixed);
+// set CNT_INTER = n_inter and clear the ghost and displaced counts
+void launch_set_counts(const LaunchCtx &lc, Inter in, int n_inter);
+void launch_pack_aos(const LaunchCtx &lc, const Geom &g, mg_atom_element *aos, Slots s, int fields, bool mixed);
+enum { PACK_ALL = 0xff, PACK_RHO = 1, PACK_DF = 2, PACK_F = 4 };
+
+void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams p, bool decide, bool mixed);
+void launch_decide_scan(const LaunchCtx &lc, const Geom &g, Slots s, Inter in);
+void launch_ghost_copy(const LaunchCtx &lc, const Geom &g, Slots s, bool mixed);
+void launch_ghost_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool mixed);
+void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook);
+void launch_lat_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook);
+void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams p, bool kick,
+                      bool mixed, bool hook);
+void launch_secondstep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams p, bool lattice);
+void launch_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed);
+// far atoms: rebuild the list from positions (uploads, hooks) and the scatter of missed pairs
+void launch_far_rebuild(const LaunchCtx &lc, const Geom &g, Slots s, Inter in);
+void launch_far_scatter(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, int kind, bool mixed);
+void set_type_maps(const int ele_of_type[3], const int pair_of_types[3][3], cudaStream_t stream);
+void launch_inter_manage(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, int steps_mask, bool mixed);
+enum { MANAGE_DECIDE = 1, MANAGE_CLEAR_GHOST = 2, MANAGE_EXCHANGE = 4, MANAGE_BORDER = 8, MANAGE_INDEX = 16 };
+void launch_inter_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed);
+void launch_inter_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed);
+void launch_inter_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed);
+void launch_inter_firststep(const LaunchCtx &lc, Inter in, StepParams p);
+void launch_setv(const LaunchCtx &lc, const Geom &g, Slots s, int64_t slot, const double dir[3], double energy);
+void launch_rescale(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const double *d_factor_src, double t_set,
+                    uint64_t n_atoms);
+// thermo reduction: out[0] mvv, out[1..3] force sum, out[4] epot, out[5] vacancies
+void launch_thermo(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool with_energy, double *partials,
+                   int n_partials, double *out);
+void launch_ws_map(const LaunchCtx &lc, const Geom &g, const double *xyz, int64_t n, int64_t *coords, uint32_t *flags,
+                   int64_t *index);
+
+}  // namespace mg

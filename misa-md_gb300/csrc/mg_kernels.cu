@@ -1,0 +1,1396 @@
+// GB300 (sm_103a) kernels for MISA-MD's per-step EAM hot path.
+//
+// Layout: structure-of-arrays over the reference's ghost-extended slot grid (doubled x), one thread
+// per local slot. The lattice density and force passes are full-neighbour gathers over the offset
+// table pruned to sites that can lie inside the cutoff (no Newton-3 scatter, no reverse fold, no
+// atomics); inter atoms (few) keep the reference's structure and add their Newton-3 share to the
+// owning lattice slot with FP64 atomics. The periodic ghost copy replaces the MPI halo exchange.
+//
+// Exact-rounding intrinsics (__dadd_rn / __dmul_rn / __ddiv_rn) are used wherever the reference's
+// result must be reproduced bit for bit: velocity-Verlet, the decide distance test, the
+// Wigner-Seitz mapping, ghost shifts and setv.
+
+#include <climits>
+#include <cstdio>
+
+#include "mg_internal.h"
+
+namespace mg {
+
+// ------------------------------------------------------------------------------------------------
+// constant tables
+// ------------------------------------------------------------------------------------------------
+__constant__ int c_full[2][kMaxFull];       // reference full offset tables (linear, per parity)
+__constant__ int c_nfull;
+// Lattice gather table: the full table reordered so that the entries whose sites are closer than
+// rc + 0.4 a0 come first (c_npruned of them). While every lattice atom is within 0.2 a0 of its site
+// (guaranteed after atom::decide) only those can hold a neighbour inside the cutoff.
+__constant__ int c_pruned[2][kMaxFull];
+__constant__ int c_npruned;
+__constant__ float c_dsite[2][kMaxFull][3];  // site_j - site_i of c_pruned entries, units a0/2
+__constant__ int c_ele_of_type[3];
+__constant__ int c_pair_of_types[3][3];
+__constant__ double c_mass[3];
+
+void set_constant_tables(const int *full_even, const int *full_odd, int n_full, const int *pruned_even,
+                         const int *pruned_odd, int n_pruned, const float *dsite_even, const float *dsite_odd,
+                         cudaStream_t stream) {
+    static int full[2][kMaxFull];
+    static int pruned[2][kMaxFull];
+    static float dsite[2][kMaxFull][3];
+    for (int i = 0; i < n_full; i++) { full[0][i] = full_even[i]; full[1][i] = full_odd[i]; }
+    for (int i = 0; i < n_full; i++) {
+        pruned[0][i] = pruned_even[i];
+        pruned[1][i] = pruned_odd[i];
+        for (int k = 0; k < 3; k++) { dsite[0][i][k] = dsite_even[3 * i + k]; dsite[1][i][k] = dsite_odd[3 * i + k]; }
+    }
+    const double mass[3] = {atom_mass(0), atom_mass(1), atom_mass(2)};
+    cudaMemcpyToSymbolAsync(c_full, full, sizeof(full), 0, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyToSymbolAsync(c_nfull, &n_full, sizeof(int), 0, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyToSymbolAsync(c_pruned, pruned, sizeof(pruned), 0, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyToSymbolAsync(c_npruned, &n_pruned, sizeof(int), 0, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyToSymbolAsync(c_dsite, dsite, sizeof(dsite), 0, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyToSymbolAsync(c_mass, mass, sizeof(mass), 0, cudaMemcpyHostToDevice, stream);
+    cudaStreamSynchronize(stream);
+}
+
+void set_type_maps(const int ele_of_type[3], const int pair_of_types[3][3], cudaStream_t stream) {
+    static int e[3];
+    static int p[3][3];
+    for (int i = 0; i < 3; i++) { e[i] = ele_of_type[i]; for (int j = 0; j < 3; j++) p[i][j] = pair_of_types[i][j]; }
+    cudaMemcpyToSymbolAsync(c_ele_of_type, e, sizeof(e), 0, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyToSymbolAsync(c_pair_of_types, p, sizeof(p), 0, cudaMemcpyHostToDevice, stream);
+    cudaStreamSynchronize(stream);
+}
+
+// ------------------------------------------------------------------------------------------------
+// index helpers
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ int lin(const Geom &g, int x, int y, int z) { return (z * g.Sy + y) * g.Sx + x; }
+
+__device__ __forceinline__ int local_slot(const Geom &g, int t, int &i, int &j, int &k) {
+    i = t % g.bx;
+    const int r = t / g.bx;
+    j = r % g.by;
+    k = r / g.by;
+    return lin(g, i + g.gx, j + g.gy, k + g.gz);
+}
+
+// The slot a ghost (or local) slot mirrors under the periodic self-exchange, with the per-dimension
+// shift the exchange adds (src/pack/lat_particle_packer.cpp:22-32: +L when sent LOWER, -L HIGHER).
+__device__ __forceinline__ int wrap_axis(int c, int g, int b, int &sgn) {
+    if (c < g) { sgn = -1; return c + b; }
+    if (c >= g + b) { sgn = 1; return c - b; }
+    sgn = 0;
+    return c;
+}
+__device__ __forceinline__ int owner_slot(const Geom &g, int s) {
+    const int X = s % g.Sx, r = s / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
+    int a, b, c;
+    return lin(g, wrap_axis(X, g.gx, g.bx, a), wrap_axis(Y, g.gy, g.by, b), wrap_axis(Z, g.gz, g.bz, c));
+}
+
+// ------------------------------------------------------------------------------------------------
+// Wigner-Seitz mapping (src/lattice/ws_utils.cpp:66-189), one rank: sub-box low corner at 0.
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ void voronoy(double X, double Y, double Z, double lc, long long &cx, long long &cy,
+                                        long long &cz) {
+    const double qx = __ddiv_rn(X, lc), qy = __ddiv_rn(Y, lc), qz = __ddiv_rn(Z, lc);
+    cx = llround(qx);
+    cy = llround(qy);
+    cz = llround(qz);
+    const double dx = __dsub_rn(qx, (double) cx);
+    const double dy = __dsub_rn(qy, (double) cy);
+    const double dz = __dsub_rn(qz, (double) cz);
+    const bool bx = dx > 0, by = dy > 0, bz = dz > 0;
+    cx = 2 * cx;
+    const double plane = __dadd_rn(__dadd_rn(__dadd_rn(bx ? dx : -dx, by ? dy : -dy), bz ? dz : -dz), -0.75);
+    if (plane >= 0.0) {
+        cx += bx ? 1 : -1;
+        cy += by ? 0 : -1;
+        cz += bz ? 0 : -1;
+    }
+}
+__device__ __forceinline__ uint32_t is_out_box(const Geom &g, double x, double y, double z) {
+    long long cx, cy, cz;
+    voronoy(x, y, z, g.a0, cx, cy, cz);
+    uint32_t f = kInBox;
+    if (cx < 0) f |= kXLow; else if (cx >= g.bx) f |= kXHigh;
+    if (cy < 0) f |= kYLow; else if (cy >= g.by) f |= kYHigh;
+    if (cz < 0) f |= kZLow; else if (cz >= g.bz) f |= kZHigh;
+    return f;
+}
+// ghost-extended coordinates of the nearest site (ws::getNearLatCoord)
+__device__ __forceinline__ void near_lat_coord(const Geom &g, double x, double y, double z, long long c[3]) {
+    voronoy(x, y, z, g.a0, c[0], c[1], c[2]);
+    c[0] += g.gx;
+    c[1] += g.gy;
+    c[2] += g.gz;
+}
+// ws::findNearLatIndexInSubBox: -1 outside the sub-box
+__device__ __forceinline__ int near_index_in_sub_box(const Geom &g, double x, double y, double z) {
+    long long cx, cy, cz;
+    voronoy(x, y, z, g.a0, cx, cy, cz);
+    if (cx < 0 || cy < 0 || cz < 0 || cx >= g.bx || cy >= g.by || cz >= g.bz) return -1;
+    return lin(g, (int) cx + g.gx, (int) cy + g.gy, (int) cz + g.gz);
+}
+// lattice site of a slot in global coordinates (decide's formula, src/atom.cpp:34-38, extended to
+// ghost slots)
+__device__ __forceinline__ void site_of(const Geom &g, int X, int Y, int Z, double &xs, double &ys, double &zs) {
+    const int i = X - g.gx, j = Y - g.gy, k = Z - g.gz;
+    const double half = (X & 1) ? 0.5 : 0.0;
+    xs = __dmul_rn((double) i * 0.5, g.a0);
+    ys = __dmul_rn((double) j + half, g.a0);
+    zs = __dmul_rn((double) k + half, g.a0);
+}
+__device__ __forceinline__ float4 make_u4(const Geom &g, double x, double y, double z, double xs, double ys,
+                                          double zs, int type) {
+    return make_float4(__double2float_rn(__dmul_rn(__dsub_rn(x, xs), g.inv_h)),
+                       __double2float_rn(__dmul_rn(__dsub_rn(y, ys), g.inv_h)),
+                       __double2float_rn(__dmul_rn(__dsub_rn(z, zs), g.inv_h)), __int_as_float(type));
+}
+
+__device__ __forceinline__ double dt_inv_m_of(const StepParams &p, int type) {
+    return type == 0 ? p.dt_inv_m[0] : (type == 1 ? p.dt_inv_m[1] : p.dt_inv_m[2]);
+}
+__device__ __forceinline__ void set_error(Inter &in, uint32_t bit) { atomicOr((unsigned *) &in.cnt[CNT_ERRORS], bit); }
+// Lattice passes can fuse df / the half-kick only when no other kernel adds density or force to
+// lattice slots afterwards: no inter atoms and no far atoms.
+__device__ __forceinline__ bool lattice_only(const Inter &in) {
+    return in.cnt[CNT_INTER] == 0 && in.cnt[CNT_FAR] == 0;
+}
+// FP64 displacement test of atom::decide (src/atom.cpp:34-42) for a local slot
+__device__ __forceinline__ bool displaced_fp64(const Geom &g, const Slots &s, int sl) {
+    const int X = sl % g.Sx, r = sl / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
+    double xs, ys, zs;
+    site_of(g, X, Y, Z, xs, ys, zs);
+    const double ex = __dsub_rn(s.x[sl], xs), ey = __dsub_rn(s.y[sl], ys), ez = __dsub_rn(s.z[sl], zs);
+    double dist = __dmul_rn(ex, ex);
+    dist = __dadd_rn(dist, __dmul_rn(ey, ey));
+    dist = __dadd_rn(dist, __dmul_rn(ez, ez));
+    return dist > g.thr;
+}
+
+// ------------------------------------------------------------------------------------------------
+// spline evaluation
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ void locate_d(double x, double inv, int n, int &m, double &p) {
+    p = x * inv;
+    m = (int) p;
+    m = max(0, min(m, n - 2));
+    p -= m;
+    p = fmin(p, 1.0);
+}
+__device__ __forceinline__ double val_d(const Knot64 *t, int m, double p) {
+    const double2 *q = reinterpret_cast<const double2 *>(t + m);
+    const double2 lo = __ldg(q), hi = __ldg(q + 1);  // {c0, c1}, {c2, c3}
+    return fma(fma(fma(hi.y, p, hi.x), p, lo.y), p, lo.x);
+}
+__device__ __forceinline__ double der_d(const Knot64 *t, int m, double p) {
+    const double2 *q = reinterpret_cast<const double2 *>(t + m);
+    const double2 lo = __ldg(q), hi = __ldg(q + 1);  // {d0, d1}, {d2, 0}
+    return fma(fma(hi.x, p, lo.y), p, lo.x);
+}
+__device__ __forceinline__ void locate_f(float x, float inv, int n, int &m, float &p) {
+    p = x * inv;
+    m = (int) p;
+    m = max(0, min(m, n - 2));
+    p -= (float) m;
+    p = fminf(p, 1.0f);
+}
+__device__ __forceinline__ float val_f(const float4 *t, int m, float p) {
+    const float4 c = __ldg(t + m);
+    return fmaf(fmaf(fmaf(c.w, p, c.z), p, c.y), p, c.x);
+}
+__device__ __forceinline__ float der_f(const float4 *t, int m, float p) {
+    const float4 c = __ldg(t + m);
+    return fmaf(fmaf(c.z, p, c.y), p, c.x);
+}
+__device__ __forceinline__ void kahan(float &sum, float &comp, float term) {
+    const float y = term - comp;
+    const float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+}
+
+// ------------------------------------------------------------------------------------------------
+// AoS <-> SoA (the reference's AtomElement array crosses the boundary as raw records)
+// ------------------------------------------------------------------------------------------------
+__global__ void k_unpack_aos(Geom g, const mg_atom_element *aos, Slots s, Inter in, int types_ok_mask, bool mixed) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n_slots) return;
+    mg_atom_element a = aos[t];
+    if (a.type < -1 || a.type > 2 || (a.type >= 0 && !((types_ok_mask >> a.type) & 1))) {
+        set_error(in, MG_DEVERR_BAD_TYPE);
+        a.type = kInvalid;
+    }
+    s.x[t] = a.x[0]; s.y[t] = a.x[1]; s.z[t] = a.x[2];
+    s.vx[t] = a.v[0]; s.vy[t] = a.v[1]; s.vz[t] = a.v[2];
+    s.fx[t] = a.f[0]; s.fy[t] = a.f[1]; s.fz[t] = a.f[2];
+    s.rho[t] = a.rho; s.df[t] = a.df;
+    s.type[t] = (int8_t) a.type;
+    s.id[t] = a.id;
+    if (mixed) {
+        const int X = t % g.Sx, r = t / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
+        double xs, ys, zs;
+        site_of(g, X, Y, Z, xs, ys, zs);
+        s.u4[t] = make_u4(g, a.x[0], a.x[1], a.x[2], xs, ys, zs, a.type);
+        s.df32[t] = (float) a.df;
+    }
+}
+
+__global__ void k_pack_aos(Geom g, mg_atom_element *aos, Slots s, int fields, bool mixed) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n_slots) return;
+    mg_atom_element &a = aos[t];
+    const double df = mixed ? (double) s.df32[t] : s.df[t];
+    if (fields == PACK_ALL) {
+        mg_atom_element b;
+        b.id = s.id[t];
+        b.type = s.type[t];
+        b.pad_ = 0;
+        b.x[0] = s.x[t]; b.x[1] = s.y[t]; b.x[2] = s.z[t];
+        b.v[0] = s.vx[t]; b.v[1] = s.vy[t]; b.v[2] = s.vz[t];
+        b.f[0] = s.fx[t]; b.f[1] = s.fy[t]; b.f[2] = s.fz[t];
+        b.rho = s.rho[t];
+        b.df = df;
+        a = b;
+        return;
+    }
+    if (fields & PACK_RHO) a.rho = s.rho[t];
+    if (fields & PACK_DF) a.df = df;
+    if (fields & PACK_F) { a.f[0] = s.fx[t]; a.f[1] = s.fy[t]; a.f[2] = s.fz[t]; }
+}
+
+void launch_unpack_aos(const LaunchCtx &lc, const Geom &g, const mg_atom_element *aos, Slots s, Inter in,
+                       int types_ok_mask, bool mixed) {
+    const int b = 256;
+    k_unpack_aos<<<(g.n_slots + b - 1) / b, b, 0, lc.stream>>>(g, aos, s, in, types_ok_mask, mixed);
+}
+__global__ void k_set_counts(Inter in, int n_inter) {
+    in.cnt[CNT_INTER] = n_inter;
+    in.cnt[CNT_GHOST] = 0;
+    in.cnt[CNT_DISPLACED] = 0;
+    *in.n_bucket = 0;
+}
+void launch_set_counts(const LaunchCtx &lc, Inter in, int n_inter) { k_set_counts<<<1, 1, 0, lc.stream>>>(in, n_inter); }
+void launch_pack_aos(const LaunchCtx &lc, const Geom &g, mg_atom_element *aos, Slots s, int fields, bool mixed) {
+    const int b = 256;
+    k_pack_aos<<<(g.n_slots + b - 1) / b, b, 0, lc.stream>>>(g, aos, s, fields, mixed);
+}
+
+// ------------------------------------------------------------------------------------------------
+// velocity-Verlet first half + drift (src/newton_motion.cpp:30-44) fused with the displacement test
+// of atom::decide (src/atom.cpp:27-53). Displaced slots are collected unordered; the list kernel
+// sorts them into the reference's k, j, i scan order.
+// ------------------------------------------------------------------------------------------------
+template <bool MOVE, bool DECIDE, bool MIXED>
+__global__ void __launch_bounds__(256) k_firststep(Geom g, Slots s, Inter in, StepParams p) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n_local) return;
+    int i, j, k;
+    const int sl = local_slot(g, t, i, j, k);
+    const int ty = s.type[sl];
+    if (ty < 0) return;
+    double x = s.x[sl], y = s.y[sl], z = s.z[sl];
+    if (MOVE) {
+        const double c = dt_inv_m_of(p, ty);
+        double vx = s.vx[sl], vy = s.vy[sl], vz = s.vz[sl];
+        vx = __dadd_rn(vx, __dmul_rn(c, s.fx[sl]));
+        vy = __dadd_rn(vy, __dmul_rn(c, s.fy[sl]));
+        vz = __dadd_rn(vz, __dmul_rn(c, s.fz[sl]));
+        x = __dadd_rn(x, __dmul_rn(p.dt, vx));
+        y = __dadd_rn(y, __dmul_rn(p.dt, vy));
+        z = __dadd_rn(z, __dmul_rn(p.dt, vz));
+        s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz;
+        s.x[sl] = x; s.y[sl] = y; s.z[sl] = z;
+    }
+    double xs, ys, zs;
+    site_of(g, i + g.gx, j + g.gy, k + g.gz, xs, ys, zs);
+    const double ex = __dsub_rn(x, xs), ey = __dsub_rn(y, ys), ez = __dsub_rn(z, zs);
+    if (MIXED && MOVE) {
+        s.u4[sl] = make_float4(__double2float_rn(__dmul_rn(ex, g.inv_h)), __double2float_rn(__dmul_rn(ey, g.inv_h)),
+                               __double2float_rn(__dmul_rn(ez, g.inv_h)), __int_as_float(ty));
+    }
+    if (DECIDE) {
+        double dist = __dmul_rn(ex, ex);
+        dist = __dadd_rn(dist, __dmul_rn(ey, ey));
+        dist = __dadd_rn(dist, __dmul_rn(ez, ez));
+        if (dist > g.thr) {
+            const int q = atomicAdd(&in.cnt[CNT_DISPLACED], 1);
+            if (q < in.dcap) in.displaced[q] = sl;
+            else set_error(in, MG_DEVERR_DISPLACED_OVERFLOW);
+        }
+    }
+}
+
+void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams p, bool decide, bool mixed) {
+    const int b = 256, n = (g.n_local + b - 1) / b;
+    if (mixed) {
+        if (decide) k_firststep<true, true, true><<<n, b, 0, lc.stream>>>(g, s, in, p);
+        else k_firststep<true, false, true><<<n, b, 0, lc.stream>>>(g, s, in, p);
+    } else {
+        if (decide) k_firststep<true, true, false><<<n, b, 0, lc.stream>>>(g, s, in, p);
+        else k_firststep<true, false, false><<<n, b, 0, lc.stream>>>(g, s, in, p);
+    }
+}
+void launch_decide_scan(const LaunchCtx &lc, const Geom &g, Slots s, Inter in) {
+    const int b = 256, n = (g.n_local + b - 1) / b;
+    StepParams p{};
+    k_firststep<false, true, false><<<n, b, 0, lc.stream>>>(g, s, in, p);
+}
+
+__global__ void k_inter_firststep(Inter in, StepParams p) {
+    const int n = in.cnt[CNT_INTER];
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
+        const double c = dt_inv_m_of(p, in.type[a]);
+        double vx = __dadd_rn(in.vx[a], __dmul_rn(c, in.fx[a]));
+        double vy = __dadd_rn(in.vy[a], __dmul_rn(c, in.fy[a]));
+        double vz = __dadd_rn(in.vz[a], __dmul_rn(c, in.fz[a]));
+        in.vx[a] = vx; in.vy[a] = vy; in.vz[a] = vz;
+        in.x[a] = __dadd_rn(in.x[a], __dmul_rn(p.dt, vx));
+        in.y[a] = __dadd_rn(in.y[a], __dmul_rn(p.dt, vy));
+        in.z[a] = __dadd_rn(in.z[a], __dmul_rn(p.dt, vz));
+    }
+}
+void launch_inter_firststep(const LaunchCtx &lc, Inter in, StepParams p) {
+    k_inter_firststep<<<lc.num_sms, 256, 0, lc.stream>>>(in, p);
+}
+
+// ------------------------------------------------------------------------------------------------
+// periodic ghost copy (replaces AtomList::exchangeAtom + LatPacker, src/atom/atom_list.cpp:51-57):
+// ghost slot <- (type, x with per-dimension +-L) of its owner. One hop reproduces the reference's
+// x -> y -> z phases exactly: each coordinate receives at most one shift.
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ int ghost_slot(const Geom &g, int t) {
+    const int nz = 2 * g.gz * g.Sy * g.Sx;
+    const int ny = 2 * g.gy * g.bz * g.Sx;
+    int X, Y, Z;
+    if (t < nz) {
+        const int plane = g.Sy * g.Sx;
+        int zz = t / plane;
+        const int r = t % plane;
+        Z = zz < g.gz ? zz : zz + g.bz;
+        Y = r / g.Sx;
+        X = r % g.Sx;
+    } else if (t < nz + ny) {
+        const int u = t - nz;
+        const int row = g.Sx;
+        const int yy = u / (g.bz * row);
+        const int r = u % (g.bz * row);
+        Y = yy < g.gy ? yy : yy + g.by;
+        Z = g.gz + r / row;
+        X = r % row;
+    } else {
+        const int u = t - nz - ny;
+        const int xx = u % (2 * g.gx);
+        const int r = u / (2 * g.gx);
+        X = xx < g.gx ? xx : xx + g.bx;
+        Y = g.gy + r % g.by;
+        Z = g.gz + r / g.by;
+    }
+    return lin(g, X, Y, Z);
+}
+
+template <bool MIXED>
+__global__ void k_ghost_copy(Geom g, Slots s) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n_ghost_slots) return;
+    const int gs = ghost_slot(g, t);
+    const int X = gs % g.Sx, r = gs / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
+    int sx, sy, sz;
+    const int os = lin(g, wrap_axis(X, g.gx, g.bx, sx), wrap_axis(Y, g.gy, g.by, sy), wrap_axis(Z, g.gz, g.bz, sz));
+    s.type[gs] = s.type[os];
+    const double ox = s.x[os], oy = s.y[os], oz = s.z[os];
+    s.x[gs] = sx ? __dadd_rn(ox, sx > 0 ? g.L[0] : -g.L[0]) : ox;
+    s.y[gs] = sy ? __dadd_rn(oy, sy > 0 ? g.L[1] : -g.L[1]) : oy;
+    s.z[gs] = sz ? __dadd_rn(oz, sz > 0 ? g.L[2] : -g.L[2]) : oz;
+    if (MIXED) s.u4[gs] = s.u4[os];
+}
+void launch_ghost_copy(const LaunchCtx &lc, const Geom &g, Slots s, bool mixed) {
+    const int b = 256, n = (g.n_ghost_slots + b - 1) / b;
+    if (mixed) k_ghost_copy<true><<<n, b, 0, lc.stream>>>(g, s);
+    else k_ghost_copy<false><<<n, b, 0, lc.stream>>>(g, s);
+}
+
+// forward df (DfEmbedPacker, src/pack/df_embed_packer.cpp): lattice ghosts and ghost inter atoms
+template <bool MIXED>
+__global__ void k_ghost_df(Geom g, Slots s, Inter in) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < g.n_ghost_slots) {
+        const int gs = ghost_slot(g, t);
+        const int os = owner_slot(g, gs);
+        if (MIXED) s.df32[gs] = s.df32[os];
+        else s.df[gs] = s.df[os];
+    }
+    const int ng = in.cnt[CNT_GHOST];
+    for (int q = t; q < ng; q += gridDim.x * blockDim.x) in.gdf[q] = in.df[in.groot[q]];
+}
+void launch_ghost_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool mixed) {
+    const int b = 256, n = (g.n_ghost_slots + b - 1) / b;
+    if (mixed) k_ghost_df<true><<<n, b, 0, lc.stream>>>(g, s, in);
+    else k_ghost_df<false><<<n, b, 0, lc.stream>>>(g, s, in);
+}
+
+// ------------------------------------------------------------------------------------------------
+// lattice density pass (atom::latRho, src/atom.cpp:151-192, as a full gather) with dF/drho fused
+// when no inter atom adds density (atom::latDf, src/atom.cpp:286-309).
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_lat_rho_fp64(Geom g, Slots s, Inter in, PotTables pt, bool hook) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n_local) return;
+    int i, j, k;
+    const int sl = local_slot(g, t, i, j, k);
+    const int ti = s.type[sl];
+    if (ti < 0) { s.rho[sl] = 0.0; return; }
+    const int par = i & 1;
+    const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
+    double acc = 0.0;
+    const int np = in.far_flag[sl] ? c_nfull : c_npruned;
+#pragma unroll 4
+    for (int q = 0; q < np; q++) {
+        const int o = par ? c_pruned[1][q] : c_pruned[0][q];
+        const int sj = sl + o;
+        const int tj = s.type[sj];
+        if (tj < 0) continue;
+        const double dx = xi - s.x[sj], dy = yi - s.y[sj], dz = zi - s.z[sj];
+        const double r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 < g.rc2) {
+            const double r = r2 * rsqrt(r2);
+            int m; double p;
+            locate_d(r, pt.inv_dr, pt.nr, m, p);
+            acc += val_d(pt.rho_v[tj], m, p);
+        }
+    }
+    s.rho[sl] = acc;
+    if (!hook && lattice_only(in)) {
+        int m; double p;
+        locate_d(acc, pt.inv_drho, pt.nrho, m, p);
+        s.df[sl] = der_d(pt.F_d[ti], m, p);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_lat_rho_mixed(Geom g, Slots s, Inter in, PotTables pt, bool hook) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n_local) return;
+    int i, j, k;
+    const int sl = local_slot(g, t, i, j, k);
+    const float4 ui = s.u4[sl];
+    const int ti = __float_as_int(ui.w);
+    if (ti < 0) { s.rho[sl] = 0.0; return; }
+    const int par = i & 1;
+    float sum = 0.f, comp = 0.f;
+    const int np = in.far_flag[sl] ? c_nfull : c_npruned;
+    const float rc2 = g.rc2_h;
+    const float hinv = pt.h_inv_dr_f;
+#pragma unroll 4
+    for (int q = 0; q < np; q++) {
+        const int o = par ? c_pruned[1][q] : c_pruned[0][q];
+        const float4 uj = __ldg(s.u4 + sl + o);
+        const int tj = __float_as_int(uj.w);
+        if (tj < 0) continue;
+        const float Dx = par ? c_dsite[1][q][0] : c_dsite[0][q][0];
+        const float Dy = par ? c_dsite[1][q][1] : c_dsite[0][q][1];
+        const float Dz = par ? c_dsite[1][q][2] : c_dsite[0][q][2];
+        const float dx = (ui.x - uj.x) - Dx, dy = (ui.y - uj.y) - Dy, dz = (ui.z - uj.z) - Dz;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 < rc2) {
+            const float rp = r2 * rsqrtf(r2);
+            int m; float p;
+            locate_f(rp, hinv, pt.nr, m, p);
+            kahan(sum, comp, val_f(pt.rho_vf[tj], m, p));
+        }
+    }
+    const double rho = (double) sum - (double) comp;
+    s.rho[sl] = rho;
+    if (!hook && lattice_only(in)) {
+        int m; float p;
+        locate_f((float) rho, pt.inv_drho_f, pt.nrho, m, p);
+        s.df32[sl] = der_f(pt.F_df[ti], m, p);
+    }
+}
+
+void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook) {
+    const int b = 256, n = (g.n_local + b - 1) / b;
+    if (mixed) k_lat_rho_mixed<<<n, b, 0, lc.stream>>>(g, s, in, t, hook);
+    else k_lat_rho_fp64<<<n, b, 0, lc.stream>>>(g, s, in, t, hook);
+}
+
+// dF/drho when inter atoms added density after the lattice pass (or for the df hook)
+template <bool MIXED>
+__global__ void k_lat_df(Geom g, Slots s, Inter in, PotTables pt, bool hook) {
+    if (!hook && lattice_only(in)) return;  // already fused into the density pass
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < g.n_local; t += gridDim.x * blockDim.x) {
+        int i, j, k;
+        const int sl = local_slot(g, t, i, j, k);
+        const int ti = s.type[sl];
+        if (ti < 0) continue;
+        if (MIXED) {
+            int m; float p;
+            locate_f((float) s.rho[sl], pt.inv_drho_f, pt.nrho, m, p);
+            s.df32[sl] = der_f(pt.F_df[ti], m, p);
+        } else {
+            int m; double p;
+            locate_d(s.rho[sl], pt.inv_drho, pt.nrho, m, p);
+            s.df[sl] = der_d(pt.F_d[ti], m, p);
+        }
+    }
+}
+void launch_lat_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook) {
+    const int b = 256;
+    const int n = hook ? (g.n_local + b - 1) / b : lc.num_sms * 8;
+    if (mixed) k_lat_df<true><<<n, b, 0, lc.stream>>>(g, s, in, t, hook);
+    else k_lat_df<false><<<n, b, 0, lc.stream>>>(g, s, in, t, hook);
+}
+
+// ------------------------------------------------------------------------------------------------
+// lattice force pass (atom::latForce, src/atom.cpp:311-358, as a full gather). When no inter atom
+// adds force, the second half-kick (NewtonMotion::secondstep, src/newton_motion.cpp:57-67) is fused.
+// fpair = -(F'_i rho'_j(r) + F'_j rho'_i(r) + phi'_ij(r)) / r, phi = (r phi)/r.
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_lat_force_fp64(Geom g, Slots s, Inter in, PotTables pt, StepParams sp,
+                                                        bool kick, bool hook) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n_local) return;
+    int i, j, k;
+    const int sl = local_slot(g, t, i, j, k);
+    const int ti = s.type[sl];
+    if (ti < 0) { s.fx[sl] = 0.0; s.fy[sl] = 0.0; s.fz[sl] = 0.0; return; }
+    const int par = i & 1;
+    const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
+    const double dfi = s.df[sl];
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    const int np = in.far_flag[sl] ? c_nfull : c_npruned;
+    const Knot64 *rho_di = pt.rho_d[ti];
+#pragma unroll 2
+    for (int q = 0; q < np; q++) {
+        const int o = par ? c_pruned[1][q] : c_pruned[0][q];
+        const int sj = sl + o;
+        const int tj = s.type[sj];
+        if (tj < 0) continue;
+        const double dx = xi - s.x[sj], dy = yi - s.y[sj], dz = zi - s.z[sj];
+        const double r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 < g.rc2) {
+            const double rinv = rsqrt(r2);
+            const double r = r2 * rinv;
+            int m; double p;
+            locate_d(r, pt.inv_dr, pt.nr, m, p);
+            const double rhojp = der_d(pt.rho_d[tj], m, p);
+            const double rhoip = (tj == ti) ? rhojp : der_d(rho_di, m, p);
+            const double zv = val_d(pt.z_v[ti][tj], m, p);
+            const double zp = der_d(pt.z_d[ti][tj], m, p);
+            const double phi = zv * rinv;
+            const double phip = zp * rinv - phi * rinv;
+            const double psip = dfi * rhojp + s.df[sj] * rhoip + phip;
+            const double fpair = -psip * rinv;
+            fx += dx * fpair;
+            fy += dy * fpair;
+            fz += dz * fpair;
+        }
+    }
+    s.fx[sl] = fx; s.fy[sl] = fy; s.fz[sl] = fz;
+    if (kick && !hook && lattice_only(in)) {
+        const double c = dt_inv_m_of(sp, ti);
+        s.vx[sl] = __dadd_rn(s.vx[sl], __dmul_rn(c, fx));
+        s.vy[sl] = __dadd_rn(s.vy[sl], __dmul_rn(c, fy));
+        s.vz[sl] = __dadd_rn(s.vz[sl], __dmul_rn(c, fz));
+    }
+}
+
+__global__ void __launch_bounds__(256) k_lat_force_mixed(Geom g, Slots s, Inter in, PotTables pt, StepParams sp,
+                                                         bool kick, bool hook) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n_local) return;
+    int i, j, k;
+    const int sl = local_slot(g, t, i, j, k);
+    const float4 ui = s.u4[sl];
+    const int ti = __float_as_int(ui.w);
+    if (ti < 0) { s.fx[sl] = 0.0; s.fy[sl] = 0.0; s.fz[sl] = 0.0; return; }
+    const int par = i & 1;
+    const float dfi = s.df32[sl];
+    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    const int np = in.far_flag[sl] ? c_nfull : c_npruned;
+    const float rc2 = g.rc2_h;
+    const float hinv = pt.h_inv_dr_f;
+    const float inv_h = 1.0f / g.h_f;
+    const float4 *rho_di = pt.rho_df_[ti];
+#pragma unroll 2
+    for (int q = 0; q < np; q++) {
+        const int o = par ? c_pruned[1][q] : c_pruned[0][q];
+        const float4 uj = __ldg(s.u4 + sl + o);
+        const int tj = __float_as_int(uj.w);
+        if (tj < 0) continue;
+        const float Dx = par ? c_dsite[1][q][0] : c_dsite[0][q][0];
+        const float Dy = par ? c_dsite[1][q][1] : c_dsite[0][q][1];
+        const float Dz = par ? c_dsite[1][q][2] : c_dsite[0][q][2];
+        const float dx = (ui.x - uj.x) - Dx, dy = (ui.y - uj.y) - Dy, dz = (ui.z - uj.z) - Dz;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 < rc2) {
+            const float rinv_h = rsqrtf(r2);
+            const float rp = r2 * rinv_h;
+            int m; float p;
+            locate_f(rp, hinv, pt.nr, m, p);
+            const float rhojp = der_f(pt.rho_df_[tj], m, p);
+            const float rhoip = (tj == ti) ? rhojp : der_f(rho_di, m, p);
+            const float zv = val_f(pt.z_vf[ti][tj], m, p);
+            const float zp = der_f(pt.z_df[ti][tj], m, p);
+            const float rinv = rinv_h * inv_h;
+            const float phi = zv * rinv;
+            const float phip = zp * rinv - phi * rinv;
+            const float psip = dfi * rhojp + __ldg(s.df32 + sl + o) * rhoip + phip;
+            const float fpair = -psip * rinv;
+            kahan(sx, cx, dx * fpair);
+            kahan(sy, cy, dy * fpair);
+            kahan(sz, cz, dz * fpair);
+        }
+    }
+    const double h = 0.5 * g.a0;
+    const double fx = h * ((double) sx - (double) cx);
+    const double fy = h * ((double) sy - (double) cy);
+    const double fz = h * ((double) sz - (double) cz);
+    s.fx[sl] = fx; s.fy[sl] = fy; s.fz[sl] = fz;
+    if (kick && !hook && lattice_only(in)) {
+        const double c = dt_inv_m_of(sp, ti);
+        s.vx[sl] = __dadd_rn(s.vx[sl], __dmul_rn(c, fx));
+        s.vy[sl] = __dadd_rn(s.vy[sl], __dmul_rn(c, fy));
+        s.vz[sl] = __dadd_rn(s.vz[sl], __dmul_rn(c, fz));
+    }
+}
+
+void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams p, bool kick,
+                      bool mixed, bool hook) {
+    const int b = 256, n = (g.n_local + b - 1) / b;
+    if (mixed) k_lat_force_mixed<<<n, b, 0, lc.stream>>>(g, s, in, t, p, kick, hook);
+    else k_lat_force_fp64<<<n, b, 0, lc.stream>>>(g, s, in, t, p, kick, hook);
+}
+
+// second half-kick for lattice slots (only when inter atoms prevented fusion, or always) and for
+// inter atoms (src/newton_motion.cpp:57-74)
+__global__ void k_secondstep(Geom g, Slots s, Inter in, StepParams p, int lattice_mode) {
+    const int n_inter = in.cnt[CNT_INTER];
+    const bool lattice = lattice_mode == 1 || (lattice_mode == 2 && !lattice_only(in));
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (lattice) {
+        for (int t = t0; t < g.n_local; t += stride) {
+            int i, j, k;
+            const int sl = local_slot(g, t, i, j, k);
+            const int ty = s.type[sl];
+            if (ty < 0) continue;
+            const double c = dt_inv_m_of(p, ty);
+            s.vx[sl] = __dadd_rn(s.vx[sl], __dmul_rn(c, s.fx[sl]));
+            s.vy[sl] = __dadd_rn(s.vy[sl], __dmul_rn(c, s.fy[sl]));
+            s.vz[sl] = __dadd_rn(s.vz[sl], __dmul_rn(c, s.fz[sl]));
+        }
+    }
+    for (int a = t0; a < n_inter; a += stride) {
+        const double c = dt_inv_m_of(p, in.type[a]);
+        in.vx[a] = __dadd_rn(in.vx[a], __dmul_rn(c, in.fx[a]));
+        in.vy[a] = __dadd_rn(in.vy[a], __dmul_rn(c, in.fy[a]));
+        in.vz[a] = __dadd_rn(in.vz[a], __dmul_rn(c, in.fz[a]));
+    }
+}
+void launch_secondstep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams p, bool lattice) {
+    k_secondstep<<<lc.num_sms * 8, 256, 0, lc.stream>>>(g, s, in, p, lattice ? 1 : 2);
+}
+
+// ------------------------------------------------------------------------------------------------
+// per-atom energy (extension): e_i = F(rho_i) + 1/2 sum_j phi_ij over lattice neighbours
+// ------------------------------------------------------------------------------------------------
+template <bool MIXED>
+__global__ void __launch_bounds__(256) k_energy(Geom g, Slots s, Inter in, PotTables pt) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n_local) return;
+    int i, j, k;
+    const int sl = local_slot(g, t, i, j, k);
+    const int ti = s.type[sl];
+    if (ti < 0) { s.e[sl] = 0.0; return; }
+    const int par = i & 1;
+    const int np = in.far_flag[sl] ? c_nfull : c_npruned;
+    if (!MIXED) {
+        const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
+        double acc = 0.0;
+        for (int q = 0; q < np; q++) {
+            const int sj = sl + (par ? c_pruned[1][q] : c_pruned[0][q]);
+            const int tj = s.type[sj];
+            if (tj < 0) continue;
+            const double dx = xi - s.x[sj], dy = yi - s.y[sj], dz = zi - s.z[sj];
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 < g.rc2) {
+                const double rinv = rsqrt(r2);
+                int m; double p;
+                locate_d(r2 * rinv, pt.inv_dr, pt.nr, m, p);
+                acc += val_d(pt.z_v[ti][tj], m, p) * rinv;
+            }
+        }
+        int m; double p;
+        locate_d(s.rho[sl], pt.inv_drho, pt.nrho, m, p);
+        s.e[sl] = val_d(pt.F_v[ti], m, p) + 0.5 * acc;
+    } else {
+        const float4 ui = s.u4[sl];
+        float sum = 0.f, comp = 0.f;
+        const float inv_h = 1.0f / g.h_f;
+        for (int q = 0; q < np; q++) {
+            const float4 uj = __ldg(s.u4 + sl + (par ? c_pruned[1][q] : c_pruned[0][q]));
+            const int tj = __float_as_int(uj.w);
+            if (tj < 0) continue;
+            const float dx = (ui.x - uj.x) - (par ? c_dsite[1][q][0] : c_dsite[0][q][0]);
+            const float dy = (ui.y - uj.y) - (par ? c_dsite[1][q][1] : c_dsite[0][q][1]);
+            const float dz = (ui.z - uj.z) - (par ? c_dsite[1][q][2] : c_dsite[0][q][2]);
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 < g.rc2_h) {
+                const float rinv_h = rsqrtf(r2);
+                int m; float p;
+                locate_f(r2 * rinv_h, pt.h_inv_dr_f, pt.nr, m, p);
+                kahan(sum, comp, val_f(pt.z_vf[ti][tj], m, p) * (rinv_h * inv_h));
+            }
+        }
+        int m; float p;
+        locate_f((float) s.rho[sl], pt.inv_drho_f, pt.nrho, m, p);
+        s.e[sl] = (double) val_f(pt.F_vf[ti], m, p) + 0.5 * ((double) sum - (double) comp);
+    }
+}
+void launch_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
+    const int b = 256, n = (g.n_local + b - 1) / b;
+    if (mixed) k_energy<true><<<n, b, 0, lc.stream>>>(g, s, in, t);
+    else k_energy<false><<<n, b, 0, lc.stream>>>(g, s, in, t);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Inter-atom list management: one block, so the reference's list order is kept exactly.
+//   decide (src/atom.cpp:21-84), exchangeInter (src/pack/inter_particle_packer.cpp),
+//   borderInter (src/pack/inter_border_packer.cpp), makeIndex (src/atom/inter_atom_list.cpp:27-45).
+// ------------------------------------------------------------------------------------------------
+constexpr int kManageThreads = 1024;
+
+// exclusive block scan of one int per thread; returns the block total
+__device__ int block_exclusive_scan(int v, int &excl) {
+    __shared__ int warp_tot[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int t = (lane < (int) (blockDim.x >> 5)) ? warp_tot[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        warp_tot[lane] = t;  // inclusive
+    }
+    __syncthreads();
+    const int warp_excl = w > 0 ? warp_tot[w - 1] : 0;
+    excl = warp_excl + x - v;
+    const int total = warp_tot[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return total;
+}
+
+// bitonic sort of n 64-bit keys in global memory by one block; buf capacity >= next pow2(n)
+__device__ void block_bitonic_sort(long long *buf, int n) {
+    int P = 1;
+    while (P < n) P <<= 1;
+    for (int i = n + threadIdx.x; i < P; i += blockDim.x) buf[i] = LLONG_MAX;
+    __syncthreads();
+    for (int kk = 2; kk <= P; kk <<= 1) {
+        for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+            for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                const int l = i ^ jj;
+                if (l > i) {
+                    const long long a = buf[i], b = buf[l];
+                    const bool up = (i & kk) == 0;
+                    if ((a > b) == up) { buf[i] = b; buf[l] = a; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// inter record move helpers (scratch layout: 13 doubles per record)
+__device__ __forceinline__ void inter_save(const Inter &in, int a, int dst) {
+    double *d = in.scratch_d + 13 * dst;
+    d[0] = in.x[a]; d[1] = in.y[a]; d[2] = in.z[a];
+    d[3] = in.vx[a]; d[4] = in.vy[a]; d[5] = in.vz[a];
+    d[6] = in.fx[a]; d[7] = in.fy[a]; d[8] = in.fz[a];
+    d[9] = in.rho[a]; d[10] = in.df[a]; d[11] = 0.0; d[12] = 0.0;
+    in.scratch_u[dst] = in.id[a];
+    in.scratch_i[dst] = in.type[a];
+}
+__device__ __forceinline__ void inter_restore(const Inter &in, int src, int a) {
+    const double *d = in.scratch_d + 13 * src;
+    in.x[a] = d[0]; in.y[a] = d[1]; in.z[a] = d[2];
+    in.vx[a] = d[3]; in.vy[a] = d[4]; in.vz[a] = d[5];
+    in.fx[a] = d[6]; in.fy[a] = d[7]; in.fz[a] = d[8];
+    in.rho[a] = d[9]; in.df[a] = d[10];
+    in.id[a] = in.scratch_u[src];
+    in.type[a] = in.scratch_i[src];
+}
+
+__device__ __forceinline__ void region_fw(const Geom &g, int d, int dir, int lo[3], int hi[3]) {
+    const int gg[3] = {g.gx, g.gy, g.gz}, bb[3] = {g.bx, g.by, g.bz}, ee[3] = {g.Sx, g.Sy, g.Sz};
+    for (int q = 0; q < 3; q++) { lo[q] = 0; hi[q] = ee[q]; }
+    for (int q = d + 1; q < 3; q++) { lo[q] = gg[q]; hi[q] = gg[q] + bb[q]; }
+    if (dir == 0) { lo[d] = gg[d]; hi[d] = 2 * gg[d]; }
+    else { lo[d] = bb[d]; hi[d] = bb[d] + gg[d]; }
+}
+
+__global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s, Inter in, int mask, bool mixed) {
+    __shared__ int sh_n;
+    const int tid = threadIdx.x, nt = blockDim.x;
+
+    if (mask & MANAGE_CLEAR_GHOST) {
+        if (tid == 0) in.cnt[CNT_GHOST] = 0;
+        __syncthreads();
+    }
+
+    if (mask & MANAGE_DECIDE) {
+        // the far list of the previous step is void: every lattice atom is re-tested below
+        {
+            const int nf = min(in.cnt[CNT_FAR], in.fcap);
+            for (int q = tid; q < nf; q += nt) in.far_flag[in.far_list[q]] = 0;
+            __syncthreads();
+            if (tid == 0) in.cnt[CNT_FAR] = 0;
+            __syncthreads();
+        }
+        // (i) displaced lattice atoms join the list in scan order
+        int nd = in.cnt[CNT_DISPLACED];
+        if (nd > in.dcap) nd = in.dcap;
+        const int n0 = in.cnt[CNT_INTER];
+        if (nd > 0) {
+            long long *keys = in.bucket;  // reused as sort buffer
+            for (int q = tid; q < nd; q += nt) keys[q] = in.displaced[q];
+            __syncthreads();
+            block_bitonic_sort(keys, nd);
+            int room = in.cap - n0;
+            if (nd > room) { if (tid == 0) set_error(in, MG_DEVERR_INTER_OVERFLOW); nd = room; }
+            for (int q = tid; q < nd; q += nt) {
+                const int sl = (int) keys[q];
+                const int a = n0 + q;
+                in.id[a] = s.id[sl];
+                in.type[a] = s.type[sl];
+                in.x[a] = s.x[sl]; in.y[a] = s.y[sl]; in.z[a] = s.z[sl];
+                in.vx[a] = s.vx[sl]; in.vy[a] = s.vy[sl]; in.vz[a] = s.vz[sl];
+                in.fx[a] = s.fx[sl]; in.fy[a] = s.fy[sl]; in.fz[a] = s.fz[sl];
+                in.rho[a] = s.rho[sl];
+                in.df[a] = mixed ? (double) s.df32[sl] : s.df[sl];
+                s.type[sl] = kInvalid;
+                s.vx[sl] = 0.0; s.vy[sl] = 0.0; s.vz[sl] = 0.0;
+                if (mixed) { float4 u = s.u4[sl]; u.w = __int_as_float(kInvalid); s.u4[sl] = u; }
+            }
+            __syncthreads();
+            if (tid == 0) in.cnt[CNT_INTER] = n0 + nd;
+        }
+        if (tid == 0) in.cnt[CNT_DISPLACED] = 0;
+        __syncthreads();
+
+        // (ii) recombination with vacancies, first claimant in list order wins
+        const int n = in.cnt[CNT_INTER];
+        int *cand = in.scratch_i + in.cap;  // n ints
+        for (int a = tid; a < n; a += nt) {
+            const int near = near_index_in_sub_box(g, in.x[a], in.y[a], in.z[a]);
+            int c = -1;
+            if (near >= 0 && s.type[near] == kInvalid && is_out_box(g, s.x[near], s.y[near], s.z[near]) == kInBox) {
+                c = near;
+                atomicMin(&in.claim[near], a);
+            }
+            cand[a] = c;
+        }
+        __syncthreads();
+        int *won = in.scratch_i + in.cap + in.cap;  // n ints
+        for (int a = tid; a < n; a += nt) won[a] = (cand[a] >= 0 && in.claim[cand[a]] == a) ? 1 : 0;
+        __syncthreads();
+        for (int a = tid; a < n; a += nt) if (cand[a] >= 0) in.claim[cand[a]] = INT_MAX;
+        for (int a = tid; a < n; a += nt) {
+            if (!won[a]) continue;
+            const int sl = cand[a];
+            s.id[sl] = in.id[a];
+            s.type[sl] = (int8_t) in.type[a];
+            s.x[sl] = in.x[a]; s.y[sl] = in.y[a]; s.z[sl] = in.z[a];
+            s.vx[sl] = in.vx[a]; s.vy[sl] = in.vy[a]; s.vz[sl] = in.vz[a];
+            if (mixed) {
+                const int X = sl % g.Sx, r = sl / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
+                double xs, ys, zs;
+                site_of(g, X, Y, Z, xs, ys, zs);
+                s.u4[sl] = make_u4(g, in.x[a], in.y[a], in.z[a], xs, ys, zs, in.type[a]);
+            }
+            // a recombined atom may sit up to sqrt(5)/4 a0 from its new site
+            if (displaced_fp64(g, s, sl)) {
+                const int q = atomicAdd(&in.cnt[CNT_FAR], 1);
+                if (q < in.fcap) { in.far_list[q] = sl; in.far_flag[sl] = 1; }
+                else set_error(in, MG_DEVERR_DISPLACED_OVERFLOW);
+            }
+        }
+        __syncthreads();
+        // stable compaction of the survivors
+        int base = 0;
+        for (int c0 = 0; c0 < n; c0 += nt) {
+            const int a = c0 + tid;
+            const int keep = (a < n && !won[a]) ? 1 : 0;
+            int ex;
+            const int tot = block_exclusive_scan(keep, ex);
+            if (keep) inter_save(in, a, base + ex);
+            base += tot;
+        }
+        __syncthreads();
+        for (int a = tid; a < base; a += nt) inter_restore(in, a, a);
+        if (tid == 0) in.cnt[CNT_INTER] = base;
+        __syncthreads();
+    }
+
+    if (mask & MANAGE_EXCHANGE) {
+        const uint32_t lowf[3] = {kXLow, kYLow, kZLow}, highf[3] = {kXHigh, kYHigh, kZHigh};
+        for (int d = 0; d < 3; d++) {
+            const int n = in.cnt[CNT_INTER];
+            int *cls = in.scratch_i + in.cap;  // 0 stay, 1 lower, 2 higher
+            for (int a = tid; a < n; a += nt) {
+                const uint32_t f = is_out_box(g, in.x[a], in.y[a], in.z[a]);
+                cls[a] = (f & lowf[d]) ? 1 : ((f & highf[d]) ? 2 : 0);
+            }
+            __syncthreads();
+            int base = 0;
+            for (int which = 0; which < 3; which++) {
+                for (int c0 = 0; c0 < n; c0 += nt) {
+                    const int a = c0 + tid;
+                    const int sel = (a < n && cls[a] == which) ? 1 : 0;
+                    int ex;
+                    const int tot = block_exclusive_scan(sel, ex);
+                    if (sel) {
+                        const int dst = base + ex;
+                        inter_save(in, a, dst);
+                        if (which != 0) {
+                            double *rec = in.scratch_d + 13 * dst;
+                            const double sh = (which == 1) ? g.L[d] : -g.L[d];
+                            rec[d] = __dadd_rn(rec[d], sh);
+                            rec[6] = 0.0; rec[7] = 0.0; rec[8] = 0.0; rec[9] = 0.0; rec[10] = 0.0;
+                        }
+                    }
+                    base += tot;
+                }
+            }
+            __syncthreads();
+            for (int a = tid; a < n; a += nt) inter_restore(in, a, a);
+            __syncthreads();
+        }
+    }
+
+    if (mask & MANAGE_BORDER) {
+        for (int d = 0; d < 3; d++) {
+            const int n_loc = in.cnt[CNT_INTER];
+            const int n_g0 = in.cnt[CNT_GHOST];
+            const int total = n_loc + n_g0;
+            for (int dir = 0; dir < 2; dir++) {
+                int lo[3], hi[3];
+                region_fw(g, d, dir, lo, hi);
+                const double sh = (dir == 0) ? g.L[d] : -g.L[d];
+                if (tid == 0) sh_n = in.cnt[CNT_GHOST];
+                __syncthreads();
+                const int base0 = sh_n;
+                int base = base0;
+                for (int c0 = 0; c0 < total; c0 += nt) {
+                    const int e = c0 + tid;
+                    int sel = 0;
+                    double px = 0, py = 0, pz = 0;
+                    int ty = 0, root = 0;
+                    if (e < total) {
+                        if (e < n_loc) { px = in.x[e]; py = in.y[e]; pz = in.z[e]; ty = in.type[e]; root = e; }
+                        else {
+                            const int q = e - n_loc;
+                            px = in.gx[q]; py = in.gy[q]; pz = in.gz[q]; ty = in.gtype[q]; root = in.groot[q];
+                        }
+                        long long c[3];
+                        near_lat_coord(g, px, py, pz, c);
+                        sel = (c[0] >= lo[0] && c[0] < hi[0] && c[1] >= lo[1] && c[1] < hi[1] && c[2] >= lo[2] &&
+                               c[2] < hi[2]) ? 1 : 0;
+                    }
+                    int ex;
+                    const int tot = block_exclusive_scan(sel, ex);
+                    if (sel) {
+                        const int q = base + ex;
+                        if (q < in.gcap) {
+                            double p3[3] = {px, py, pz};
+                            p3[d] = __dadd_rn(p3[d], sh);
+                            in.gx[q] = p3[0]; in.gy[q] = p3[1]; in.gz[q] = p3[2];
+                            in.gtype[q] = ty;
+                            in.groot[q] = root;
+                            in.gdf[q] = 0.0;
+                        } else {
+                            set_error(in, MG_DEVERR_GHOST_OVERFLOW);
+                        }
+                    }
+                    base += tot;
+                }
+                __syncthreads();
+                if (tid == 0) in.cnt[CNT_GHOST] = base < in.gcap ? base : in.gcap;
+                __syncthreads();
+            }
+        }
+    }
+
+    if (mask & MANAGE_INDEX) {
+        const int n_loc = in.cnt[CNT_INTER];
+        const int n_gh = in.cnt[CNT_GHOST];
+        const int total = n_loc + n_gh;
+        for (int e = tid; e < total; e += nt) {
+            double px, py, pz;
+            int ref;
+            if (e < n_loc) { px = in.x[e]; py = in.y[e]; pz = in.z[e]; ref = e; }
+            else { const int q = e - n_loc; px = in.gx[q]; py = in.gy[q]; pz = in.gz[q]; ref = in.cap + q; }
+            long long c[3];
+            near_lat_coord(g, px, py, pz, c);
+            long long key;
+            if (c[0] < 0 || c[1] < 0 || c[2] < 0 || c[0] >= g.Sx || c[1] >= g.Sy || c[2] >= g.Sz) {
+                set_error(in, MG_DEVERR_OUT_OF_GRID);
+                key = INT_MAX;
+            } else {
+                key = lin(g, (int) c[0], (int) c[1], (int) c[2]);
+            }
+            in.bucket[e] = (key << 32) | (long long) ref;
+        }
+        __syncthreads();
+        block_bitonic_sort(in.bucket, total);
+        if (tid == 0) *in.n_bucket = total;
+    }
+}
+
+void launch_inter_manage(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, int mask, bool mixed) {
+    k_inter_manage<<<1, kManageThreads, 0, lc.stream>>>(g, s, in, mask, mixed);
+}
+
+// ------------------------------------------------------------------------------------------------
+// inter-atom EAM (atom::interRho / interForce, src/atom.cpp:194-284, 360-473), FP64 arithmetic.
+// One thread per local inter atom; Newton-3 shares go to the owning lattice slot by FP64 atomics.
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ int bucket_begin(const Inter &in, int nb, int key) {
+    int lo = 0, hi = nb;
+    const long long want = ((long long) key) << 32;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (in.bucket[mid] < want) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+struct InterRef {
+    double x, y, z, df;
+    int type;
+    uint64_t id;
+};
+__device__ __forceinline__ InterRef inter_ref(const Inter &in, int ref) {
+    InterRef r;
+    if (ref < in.cap) { r.x = in.x[ref]; r.y = in.y[ref]; r.z = in.z[ref]; r.type = in.type[ref]; r.id = in.id[ref]; r.df = in.df[ref]; }
+    else {
+        const int q = ref - in.cap;
+        r.x = in.gx[q]; r.y = in.gy[q]; r.z = in.gz[q]; r.type = in.gtype[q]; r.id = 0; r.df = in.gdf[q];
+    }
+    return r;
+}
+__device__ __forceinline__ double rho_fn(const PotTables &pt, int type, double r2) {
+    int m; double p;
+    locate_d(sqrt(r2), pt.inv_dr, pt.nr, m, p);
+    return val_d(pt.rho_v[type], m, p);
+}
+__device__ __forceinline__ double to_force(const PotTables &pt, int ti, int tj, double r2, double dfi, double dfj) {
+    const double r = sqrt(r2);
+    int m; double p;
+    locate_d(r, pt.inv_dr, pt.nr, m, p);
+    const double rhoip = der_d(pt.rho_d[ti], m, p);
+    const double rhojp = der_d(pt.rho_d[tj], m, p);
+    const double zv = val_d(pt.z_v[ti][tj], m, p);
+    const double zp = der_d(pt.z_d[ti][tj], m, p);
+    const double recip = 1.0 / r;
+    const double phi = zv * recip;
+    const double phip = zp * recip - phi * recip;
+    const double psip = dfi * rhojp + dfj * rhoip + phip;
+    return -psip * recip;
+}
+__device__ __forceinline__ double pair_fn(const PotTables &pt, int ti, int tj, double r2) {
+    const double r = sqrt(r2);
+    int m; double p;
+    locate_d(r, pt.inv_dr, pt.nr, m, p);
+    return val_d(pt.z_v[ti][tj], m, p) / r;
+}
+__device__ __forceinline__ double lat_df(const Slots &s, int sl, bool mixed) { return mixed ? (double) s.df32[sl] : s.df[sl]; }
+
+// kind: 0 density, 1 force, 2 energy
+template <int KIND>
+__global__ void k_inter_eam(Geom g, Slots s, Inter in, PotTables pt, bool mixed) {
+    const int n = in.cnt[CNT_INTER];
+    const int nb = *in.n_bucket;
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
+        const double xa = in.x[a], ya = in.y[a], za = in.z[a];
+        const int ta = in.type[a];
+        const uint64_t ida = in.id[a];
+        const double dfa = in.df[a];
+        const int near = near_index_in_sub_box(g, xa, ya, za);
+        if (near < 0) continue;
+        double acc = 0.0, fx = 0.0, fy = 0.0, fz = 0.0;
+        // lattice partners: the nearest site's atom, then the full offsets of that site
+        const int par = (near % g.Sx) & 1;
+        const int nf = c_nfull;
+        for (int q = -1; q < nf; q++) {
+            const int sj = q < 0 ? near : near + (par ? c_full[1][q] : c_full[0][q]);
+            if (sj < 0 || sj >= g.n_slots) { set_error(in, MG_DEVERR_OUT_OF_GRID); continue; }
+            const int tj = s.type[sj];
+            if (tj < 0) continue;
+            const double dx = xa - s.x[sj], dy = ya - s.y[sj], dz = za - s.z[sj];
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            if (!(r2 < g.rc2)) continue;
+            const int own = owner_slot(g, sj);
+            if (KIND == 0) {
+                acc += rho_fn(pt, tj, r2);
+                atomicAdd(&s.rho[own], rho_fn(pt, ta, r2));
+            } else if (KIND == 1) {
+                const double fp = to_force(pt, ta, tj, r2, dfa, lat_df(s, sj, mixed));
+                fx += dx * fp; fy += dy * fp; fz += dz * fp;
+                atomicAdd(&s.fx[own], -dx * fp);
+                atomicAdd(&s.fy[own], -dy * fp);
+                atomicAdd(&s.fz[own], -dz * fp);
+            } else {
+                const double h = 0.5 * pair_fn(pt, ta, tj, r2);
+                acc += h;
+                atomicAdd(&s.e[own], h);
+            }
+        }
+        // inter partners: same-site bucket (not itself), then the buckets of the full offsets
+        for (int q = -1; q < nf; q++) {
+            const int key = q < 0 ? near : near + (par ? c_full[1][q] : c_full[0][q]);
+            for (int b = bucket_begin(in, nb, key); b < nb && (int) (in.bucket[b] >> 32) == key; b++) {
+                const InterRef o = inter_ref(in, (int) (in.bucket[b] & 0xffffffffLL));
+                if (q < 0 && o.id == ida) continue;
+                const double dx = xa - o.x, dy = ya - o.y, dz = za - o.z;
+                const double r2 = dx * dx + dy * dy + dz * dz;
+                if (!(r2 < g.rc2)) continue;
+                if (KIND == 0) acc += rho_fn(pt, o.type, r2);
+                else if (KIND == 1) {
+                    const double fp = to_force(pt, ta, o.type, r2, dfa, o.df);
+                    fx += dx * fp; fy += dy * fp; fz += dz * fp;
+                } else {
+                    acc += 0.5 * pair_fn(pt, ta, o.type, r2);
+                }
+            }
+        }
+        if (KIND == 0) {
+            in.rho[a] = acc;
+            int m; double p;
+            locate_d(acc, pt.inv_drho, pt.nrho, m, p);
+            in.df[a] = der_d(pt.F_d[ta], m, p);
+        } else if (KIND == 1) {
+            in.fx[a] = fx; in.fy[a] = fy; in.fz[a] = fz;
+        } else {
+            int m; double p;
+            locate_d(in.rho[a], pt.inv_drho, pt.nrho, m, p);
+            in.e[a] = val_d(pt.F_v[ta], m, p) + acc;
+        }
+    }
+}
+void launch_inter_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
+    k_inter_eam<0><<<lc.num_sms, 128, 0, lc.stream>>>(g, s, in, t, mixed);
+}
+void launch_inter_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
+    k_inter_eam<1><<<lc.num_sms, 128, 0, lc.stream>>>(g, s, in, t, mixed);
+}
+void launch_inter_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
+    k_inter_eam<2><<<lc.num_sms, 128, 0, lc.stream>>>(g, s, in, t, mixed);
+}
+
+// ------------------------------------------------------------------------------------------------
+// far lattice atoms (farther than 0.2 a0 from their site). Rebuild from positions for states that did
+// not come through atom::decide (uploads, the per-phase hooks).
+// ------------------------------------------------------------------------------------------------
+__global__ void k_far_clear(Inter in) {
+    const int nf = min(in.cnt[CNT_FAR], in.fcap);
+    for (int q = threadIdx.x; q < nf; q += blockDim.x) in.far_flag[in.far_list[q]] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) in.cnt[CNT_FAR] = 0;
+}
+__global__ void k_far_scan(Geom g, Slots s, Inter in) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n_local) return;
+    int i, j, k;
+    const int sl = local_slot(g, t, i, j, k);
+    if (s.type[sl] < 0) return;
+    if (displaced_fp64(g, s, sl)) {
+        const int q = atomicAdd(&in.cnt[CNT_FAR], 1);
+        if (q < in.fcap) { in.far_list[q] = sl; in.far_flag[sl] = 1; }
+        else set_error(in, MG_DEVERR_DISPLACED_OVERFLOW);
+    }
+}
+void launch_far_rebuild(const LaunchCtx &lc, const Geom &g, Slots s, Inter in) {
+    k_far_clear<<<1, 1024, 0, lc.stream>>>(in);
+    const int b = 256;
+    k_far_scan<<<(g.n_local + b - 1) / b, b, 0, lc.stream>>>(g, s, in);
+}
+
+// Pairs between a far atom i and a lattice atom j whose sites are beyond the pruned radius: j's
+// pruned gather does not see them, so i adds j's share (FP64, to j's owner). Skipped when j's owner
+// is itself far (its full gather sees i). kind: 0 density, 1 force, 2 energy.
+template <int KIND>
+__global__ void k_far_scatter(Geom g, Slots s, Inter in, PotTables pt, bool mixed) {
+    const int nf = min(in.cnt[CNT_FAR], in.fcap);
+    const int nfull = c_nfull, np = c_npruned;
+    for (int q0 = blockIdx.x * blockDim.x + threadIdx.x; q0 < nf; q0 += gridDim.x * blockDim.x) {
+        const int sl = in.far_list[q0];
+        const int ti = s.type[sl];
+        if (ti < 0) continue;
+        const int par = (sl % g.Sx) & 1;
+        const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
+        const double dfi = mixed ? (double) s.df32[sl] : s.df[sl];
+        for (int q = np; q < nfull; q++) {
+            const int sj = sl + (par ? c_pruned[1][q] : c_pruned[0][q]);
+            const int tj = s.type[sj];
+            if (tj < 0) continue;
+            const int own = owner_slot(g, sj);
+            if (in.far_flag[own]) continue;
+            const double dx = xi - s.x[sj], dy = yi - s.y[sj], dz = zi - s.z[sj];
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            if (!(r2 < g.rc2)) continue;
+            const double r = sqrt(r2);
+            int m; double p;
+            locate_d(r, pt.inv_dr, pt.nr, m, p);
+            if (KIND == 0) {
+                atomicAdd(&s.rho[own], val_d(pt.rho_v[ti], m, p));
+            } else if (KIND == 1) {
+                const double dfj = mixed ? (double) s.df32[sj] : s.df[sj];
+                const double rhoip = der_d(pt.rho_d[ti], m, p), rhojp = der_d(pt.rho_d[tj], m, p);
+                const double zv = val_d(pt.z_v[ti][tj], m, p), zp = der_d(pt.z_d[ti][tj], m, p);
+                const double recip = 1.0 / r;
+                const double phi = zv * recip;
+                const double phip = zp * recip - phi * recip;
+                const double fp = -(dfi * rhojp + dfj * rhoip + phip) * recip;
+                atomicAdd(&s.fx[own], -dx * fp);
+                atomicAdd(&s.fy[own], -dy * fp);
+                atomicAdd(&s.fz[own], -dz * fp);
+            } else {
+                atomicAdd(&s.e[own], 0.5 * val_d(pt.z_v[ti][tj], m, p) / r);
+            }
+        }
+    }
+}
+void launch_far_scatter(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, int kind, bool mixed) {
+    if (kind == 0) k_far_scatter<0><<<lc.num_sms, 128, 0, lc.stream>>>(g, s, in, t, mixed);
+    else if (kind == 1) k_far_scatter<1><<<lc.num_sms, 128, 0, lc.stream>>>(g, s, in, t, mixed);
+    else k_far_scatter<2><<<lc.num_sms, 128, 0, lc.stream>>>(g, s, in, t, mixed);
+}
+
+// ------------------------------------------------------------------------------------------------
+// setv (src/atom.cpp:475-494): one thread
+// ------------------------------------------------------------------------------------------------
+__global__ void k_setv(Slots s, int slot, double dir0, double dir1, double dir2, double energy) {
+    const int ty = s.type[slot];
+    const double m = (ty >= 0 && ty < 3) ? c_mass[ty] : 0.0;
+    const double v_ = __dsqrt_rn(__ddiv_rn(__ddiv_rn(__dmul_rn(2.0, energy), m), kMvv2e));
+    const double d_ = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dir0, dir0), __dmul_rn(dir1, dir1)), __dmul_rn(dir2, dir2)));
+    s.vx[slot] = __dadd_rn(s.vx[slot], __ddiv_rn(__dmul_rn(v_, dir0), d_));
+    s.vy[slot] = __dadd_rn(s.vy[slot], __ddiv_rn(__dmul_rn(v_, dir1), d_));
+    s.vz[slot] = __dadd_rn(s.vz[slot], __ddiv_rn(__dmul_rn(v_, dir2), d_));
+}
+void launch_setv(const LaunchCtx &lc, const Geom &g, Slots s, int64_t slot, const double dir[3], double energy) {
+    k_setv<<<1, 1, 0, lc.stream>>>(s, (int) slot, dir[0], dir[1], dir[2], energy);
+}
+
+// rescale (src/system_configuration.cpp:321-346): factor = sqrt(T / T_now) from the mvv reduction
+__global__ void k_rescale(Geom g, Slots s, Inter in, const double *mvv, double t_set, uint64_t n_atoms) {
+    const uint64_t dof = 3 * n_atoms - 3;
+    const double scalar = __ddiv_rn(__dmul_rn(*mvv, kMvv2e), __dmul_rn((double) dof, kBoltz));
+    const double f = __dsqrt_rn(__ddiv_rn(t_set, scalar));
+    const int stride = gridDim.x * blockDim.x;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < g.n_local; t += stride) {
+        int i, j, k;
+        const int sl = local_slot(g, t, i, j, k);
+        s.vx[sl] = __dmul_rn(s.vx[sl], f);
+        s.vy[sl] = __dmul_rn(s.vy[sl], f);
+        s.vz[sl] = __dmul_rn(s.vz[sl], f);
+    }
+    const int n = in.cnt[CNT_INTER];
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += stride) {
+        in.vx[a] = __dmul_rn(in.vx[a], f);
+        in.vy[a] = __dmul_rn(in.vy[a], f);
+        in.vz[a] = __dmul_rn(in.vz[a], f);
+    }
+}
+void launch_rescale(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const double *d_mvv, double t_set,
+                    uint64_t n_atoms) {
+    k_rescale<<<lc.num_sms * 8, 256, 0, lc.stream>>>(g, s, in, d_mvv, t_set, n_atoms);
+}
+
+// ------------------------------------------------------------------------------------------------
+// thermo reduction (deterministic: per-block partials, then one block in fixed order)
+// out: [0] sum m v^2, [1..3] force sum, [4] potential energy, [5] vacancies
+// ------------------------------------------------------------------------------------------------
+constexpr int kThermoWords = 6;
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__global__ void __launch_bounds__(256) k_thermo_partial(Geom g, Slots s, Inter in, bool with_energy, double *partials) {
+    double acc[kThermoWords] = {0, 0, 0, 0, 0, 0};
+    const int stride = gridDim.x * blockDim.x;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < g.n_local; t += stride) {
+        int i, j, k;
+        const int sl = local_slot(g, t, i, j, k);
+        const int ty = s.type[sl];
+        if (ty < 0) { acc[5] += 1.0; continue; }
+        const double vx = s.vx[sl], vy = s.vy[sl], vz = s.vz[sl];
+        acc[0] += (vx * vx + vy * vy + vz * vz) * c_mass[ty];
+        acc[1] += s.fx[sl]; acc[2] += s.fy[sl]; acc[3] += s.fz[sl];
+        if (with_energy) acc[4] += s.e[sl];
+    }
+    if (blockIdx.x == 0) {
+        const int n = in.cnt[CNT_INTER];
+        for (int a = threadIdx.x; a < n; a += blockDim.x) {
+            const double vx = in.vx[a], vy = in.vy[a], vz = in.vz[a];
+            acc[0] += (vx * vx + vy * vy + vz * vz) * c_mass[in.type[a]];
+            acc[1] += in.fx[a]; acc[2] += in.fy[a]; acc[3] += in.fz[a];
+            if (with_energy) acc[4] += in.e[a];
+        }
+    }
+    __shared__ double sh[kThermoWords][8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int q = 0; q < kThermoWords; q++) {
+        const double v = warp_sum(acc[q]);
+        if (lane == 0) sh[q][w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kThermoWords) {
+        double v = 0;
+        for (int q = 0; q < (int) (blockDim.x >> 5); q++) v += sh[threadIdx.x][q];
+        partials[blockIdx.x * kThermoWords + threadIdx.x] = v;
+    }
+}
+__global__ void k_thermo_final(const double *partials, int nb, double *out) {
+    if (threadIdx.x < kThermoWords) {
+        double v = 0;
+        for (int b = 0; b < nb; b++) v += partials[b * kThermoWords + threadIdx.x];
+        out[threadIdx.x] = v;
+    }
+}
+void launch_thermo(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool with_energy, double *partials,
+                   int n_partials, double *out) {
+    k_thermo_partial<<<n_partials, 256, 0, lc.stream>>>(g, s, in, with_energy, partials);
+    k_thermo_final<<<1, 32, 0, lc.stream>>>(partials, n_partials, out);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Wigner-Seitz mapping of arbitrary points (indexing parity checks)
+// ------------------------------------------------------------------------------------------------
+__global__ void k_ws_map(Geom g, const double *xyz, int64_t n, int64_t *coords, uint32_t *flags, int64_t *index) {
+    const int64_t t = blockIdx.x * (int64_t) blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const double x = xyz[3 * t], y = xyz[3 * t + 1], z = xyz[3 * t + 2];
+    long long c[3];
+    near_lat_coord(g, x, y, z, c);
+    coords[3 * t] = c[0]; coords[3 * t + 1] = c[1]; coords[3 * t + 2] = c[2];
+    flags[t] = is_out_box(g, x, y, z);
+    index[t] = near_index_in_sub_box(g, x, y, z);
+}
+void launch_ws_map(const LaunchCtx &lc, const Geom &g, const double *xyz, int64_t n, int64_t *coords, uint32_t *flags,
+                   int64_t *index) {
+    const int b = 256;
+    k_ws_map<<<(unsigned) ((n + b - 1) / b), b, 0, lc.stream>>>(g, xyz, n, coords, flags, index);
+}
+
+}  // namespace mg

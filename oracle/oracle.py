@@ -1,0 +1,257 @@
+"""TEST INFRASTRUCTURE - NOT PART OF THE PRODUCT.
+
+ctypes binding of the CPU oracle (oracle/misa_oracle.cpp), the single-rank restatement of MISA-MD's
+EAM hot path. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it, as the
+checker or the timed CPU baseline; the product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+ATOM_DTYPE = np.dtype(
+    [("id", "<u8"), ("type", "<i4"), ("pad_", "<i4"), ("x", "<f8", (3,)), ("v", "<f8", (3,)),
+     ("f", "<f8", (3,)), ("rho", "<f8"), ("df", "<f8")],
+    align=True,
+)
+
+
+class DomainDesc(ctypes.Structure):
+    _fields_ = [("phase_space", ctypes.c_int64 * 3), ("lattice_const", ctypes.c_double),
+                ("cutoff_radius_factor", ctypes.c_double), ("grid_size", ctypes.c_int32 * 3),
+                ("grid_coord", ctypes.c_int32 * 3), ("ghost_size", ctypes.c_int32)]
+
+
+def build(force=False):
+    src = os.path.join(HERE, "misa_oracle.cpp")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(src) > os.path.getmtime(LIB_PATH) or \
+            os.path.getmtime(os.path.join(HERE, "misa_oracle.h")) > os.path.getmtime(LIB_PATH):
+        subprocess.run(["make", "-s", "-C", HERE, "-B" if force else "_build/liboracle.so"], check=True)
+    return LIB_PATH
+
+
+_LIB = None
+_P, _I32, _I64, _U64, _D = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64, ctypes.c_double
+_PROTOS = {
+    "orc_ws_near_lat_sub_box_coord": (None, [_P, _P, _P]),
+    "orc_ws_near_lat_coord": (None, [_P, _P, _P]),
+    "orc_ws_is_out_box": (ctypes.c_uint32, [_P, _P]),
+    "orc_ws_find_near_lat_index_in_sub_box": (_I64, [_P, _P]),
+    "orc_ws_batch": (None, [_P, _P, _I64, _P, _P, _P, _P]),
+    "orc_nei_offsets": (_I32, [_I64, _I64, _I64, _I32, _D, _I32, _P, _I32]),
+    "orc_is_positive_index": (_I32, [_D, _D, _D]),
+    "orc_create": (_P, [_P, _D, _D, ctypes.c_char_p, _D]),
+    "orc_destroy": (None, [_P]),
+    "orc_last_error": (ctypes.c_char_p, []),
+    "orc_grid": (None, [_P, _P]),
+    "orc_n_slots": (_I64, [_P]),
+    "orc_set_atoms": (None, [_P, _P, _I64]),
+    "orc_get_atoms": (None, [_P, _P, _I64]),
+    "orc_get_inter": (_I64, [_P, _P, _I64]),
+    "orc_get_ghost_inter": (_I64, [_P, _P, _I64]),
+    "orc_set_inter": (None, [_P, _P, _I64]),
+    "orc_set_timestep": (None, [_P, _D]),
+    "orc_firststep": (None, [_P]),
+    "orc_decide": (_I32, [_P]),
+    "orc_exchange_inter": (None, [_P]),
+    "orc_border_inter": (None, [_P]),
+    "orc_exchange_atom_first": (None, [_P]),
+    "orc_exchange_atom": (None, [_P]),
+    "orc_clear_force": (None, [_P]),
+    "orc_compute_eam": (None, [_P]),
+    "orc_secondstep": (None, [_P]),
+    "orc_prepare": (None, [_P]),
+    "orc_simulate": (None, [_P, _I64]),
+    "orc_collision_step": (None, [_P, _P, _P, _D]),
+    "orc_setv": (None, [_P, _P, _P, _D]),
+    "orc_mvv": (_D, [_P]),
+    "orc_kinetic_energy": (_D, [_P]),
+    "orc_temperature": (_D, [_P, _U64]),
+    "orc_rescale": (None, [_P, _D, _U64]),
+    "orc_system_force": (None, [_P, _P]),
+    "orc_potential_energy": (_D, [_P, _P, _P, _I64]),
+    "orc_pot_charge_density": (_D, [_P, _I32, _D]),
+    "orc_pot_d_embed": (_D, [_P, _I32, _D]),
+    "orc_pot_embed": (_D, [_P, _I32, _D]),
+    "orc_pot_to_force": (_D, [_P, _I32, _I32, _D, _D, _D]),
+    "orc_pot_pair": (_D, [_P, _I32, _I32, _D]),
+    "orc_pot_spline": (_I32, [_P, _I32, _I32, _I32, _P, _I32]),
+    "orc_time_simulate": (_D, [_P, _I64]),
+}
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _PROTOS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def domain_desc(phase_space, lattice_const, cutoff_radius_factor, grid_size=(1, 1, 1), grid_coord=(0, 0, 0),
+                ghost_size=0):
+    d = DomainDesc()
+    for i in range(3):
+        d.phase_space[i] = int(phase_space[i])
+        d.grid_size[i] = int(grid_size[i])
+        d.grid_coord[i] = int(grid_coord[i])
+    d.lattice_const = float(lattice_const)
+    d.cutoff_radius_factor = float(cutoff_radius_factor)
+    d.ghost_size = int(ghost_size)
+    return d
+
+
+def ws_near_lat_sub_box_coord(desc, x):
+    out = np.zeros(3, dtype=np.int64)
+    xx = np.asarray(x, dtype=np.float64)
+    lib().orc_ws_near_lat_sub_box_coord(ctypes.byref(desc), _ptr(xx), _ptr(out))
+    return out
+
+
+def ws_near_lat_coord(desc, x):
+    out = np.zeros(3, dtype=np.int64)
+    xx = np.asarray(x, dtype=np.float64)
+    lib().orc_ws_near_lat_coord(ctypes.byref(desc), _ptr(xx), _ptr(out))
+    return out
+
+
+def ws_is_out_box(desc, x):
+    xx = np.asarray(x, dtype=np.float64)
+    return int(lib().orc_ws_is_out_box(ctypes.byref(desc), _ptr(xx)))
+
+
+def ws_find_near_lat_index_in_sub_box(desc, x):
+    xx = np.asarray(x, dtype=np.float64)
+    return int(lib().orc_ws_find_near_lat_index_in_sub_box(ctypes.byref(desc), _ptr(xx)))
+
+
+def ws_batch(desc, xyz):
+    """Vectorised Wigner-Seitz mapping: (ext_coords, sub_coords, flags, index)."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    n = xyz.shape[0]
+    ext = np.zeros((n, 3), dtype=np.int64)
+    sub = np.zeros((n, 3), dtype=np.int64)
+    flags = np.zeros(n, dtype=np.uint32)
+    index = np.zeros(n, dtype=np.int64)
+    lib().orc_ws_batch(ctypes.byref(desc), _ptr(xyz), n, _ptr(ext), _ptr(sub), _ptr(flags), _ptr(index))
+    return ext, sub, flags, index
+
+
+def nei_offsets(size_x, size_y, size_z, cut_lattice, cutoff_radius_factor, which):
+    n = lib().orc_nei_offsets(size_x, size_y, size_z, cut_lattice, cutoff_radius_factor, which, None, 0)
+    out = np.zeros(n, dtype=np.int64)
+    lib().orc_nei_offsets(size_x, size_y, size_z, cut_lattice, cutoff_radius_factor, which, _ptr(out), n)
+    return out
+
+
+def is_positive_index(x, y, z):
+    return bool(lib().orc_is_positive_index(x, y, z))
+
+
+class OracleSim:
+    """Single-rank CPU restatement of the reference's simulation state."""
+
+    def __init__(self, cells, lattice_const, cutoff_radius_factor, setfl_path, dt=0.001):
+        L = lib()
+        ps = np.asarray(cells, dtype=np.int64)
+        self.h = L.orc_create(_ptr(ps), float(lattice_const), float(cutoff_radius_factor),
+                              os.fsencode(setfl_path), float(dt))
+        if not self.h:
+            raise RuntimeError("oracle: " + L.orc_last_error().decode())
+        g = np.zeros(6, dtype=np.int64)
+        L.orc_grid(self.h, _ptr(g))
+        self.grid = tuple(int(v) for v in g)
+        self.n_slots = int(L.orc_n_slots(self.h))
+        self.L = L
+
+    def close(self):
+        if self.h:
+            self.L.orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_atoms(self, atoms):
+        atoms = np.ascontiguousarray(atoms, dtype=ATOM_DTYPE)
+        assert atoms.size == self.n_slots
+        self.L.orc_set_atoms(self.h, _ptr(atoms), atoms.size)
+
+    def get_atoms(self):
+        out = np.zeros(self.n_slots, dtype=ATOM_DTYPE)
+        self.L.orc_get_atoms(self.h, _ptr(out), out.size)
+        return out
+
+    def get_inter(self):
+        n = self.L.orc_get_inter(self.h, None, 0)
+        out = np.zeros(n, dtype=ATOM_DTYPE)
+        if n:
+            self.L.orc_get_inter(self.h, _ptr(out), n)
+        return out
+
+    def get_ghost_inter(self):
+        n = self.L.orc_get_ghost_inter(self.h, None, 0)
+        out = np.zeros(n, dtype=ATOM_DTYPE)
+        if n:
+            self.L.orc_get_ghost_inter(self.h, _ptr(out), n)
+        return out
+
+    def set_inter(self, inter):
+        inter = np.ascontiguousarray(inter, dtype=ATOM_DTYPE)
+        self.L.orc_set_inter(self.h, _ptr(inter) if inter.size else None, inter.size)
+
+    def set_timestep(self, dt):
+        self.L.orc_set_timestep(self.h, float(dt))
+
+    def __getattr__(self, name):
+        # thin pass-through for the step pieces: firststep, decide, exchange_inter, ...
+        fn = getattr(lib(), "orc_" + name, None)
+        if fn is None or name.startswith("_"):
+            raise AttributeError(name)
+        return lambda *a: fn(self.h, *a)
+
+    def collision_step(self, lat, direction, energy):
+        lat = np.asarray(lat, dtype=np.int32)
+        d = np.asarray(direction, dtype=np.float64)
+        self.L.orc_collision_step(self.h, _ptr(lat), _ptr(d), float(energy))
+
+    def setv(self, lat, direction, energy):
+        lat = np.asarray(lat, dtype=np.int32)
+        d = np.asarray(direction, dtype=np.float64)
+        self.L.orc_setv(self.h, _ptr(lat), _ptr(d), float(energy))
+
+    def system_force(self):
+        out = np.zeros(3)
+        self.L.orc_system_force(self.h, _ptr(out))
+        return out
+
+    def potential_energy(self, per_slot=False, inter_cap=0):
+        e = np.zeros(self.n_slots) if per_slot else None
+        ei = np.zeros(inter_cap) if inter_cap else None
+        total = self.L.orc_potential_energy(self.h, _ptr(e), _ptr(ei), inter_cap)
+        return total, e, ei
+
+    def pot_spline(self, kind, e1, e2=0):
+        n = self.L.orc_pot_spline(self.h, kind, e1, e2, None, 0)
+        out = np.zeros(7 * n)
+        self.L.orc_pot_spline(self.h, kind, e1, e2, _ptr(out), out.size)
+        return out.reshape(n, 7)
