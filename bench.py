@@ -52,6 +52,10 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cells", type=int, default=0, help="override the workload's unit cells per edge")
+    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    p.add_argument("--resident-only", action="store_true",
+                   help="time only the resident step (no accuracy, FP64, drift, e2e or CPU legs)")
     return p.parse_args()
 
 
@@ -215,6 +219,9 @@ def run_ours(args):
     pkg.load_library()
     wl = pkg.workloads
     w = wl.WORKLOADS[args.workload]
+    if args.cells:
+        import dataclasses
+        w = dataclasses.replace(w, cells=(args.cells,) * 3, name=f"{w.name}@{args.cells}c")
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -238,8 +245,8 @@ def run_ours(args):
         c.prepare()
         return c
 
-    # ---- mixed precision, resident ----
-    ctx = make_ctx("mixed")
+    # ---- resident ----
+    ctx = make_ctx(args.precision)
     ctx.simulate(args.warmup, sync=True)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=device)
     ctx.enable_timing(True)
@@ -268,6 +275,13 @@ def run_ours(args):
     force_ms = kt.get("lat_force", float("nan"))
     achieved = BYTES_PER_ATOM_FORCE_SWEEP * n_atoms / (force_ms / 1e3) / 1e9
     step_achieved = BYTES_PER_ATOM_STEP * n_atoms / (ms_per_step / 1e3) / 1e9
+    if args.resident_only:
+        ctx.close()
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                              "ms_per_step": ms_per_step, "precision": args.precision, "workload": w.name,
+                              "kernel_ms_per_step": kt, "roofline_achieved_gbs": achieved, "clocks": clocks}))
+        return
 
     # ---- accuracy of the mixed form against the FP64 form on the same state ----
     ctx64 = make_ctx("fp64")

@@ -176,54 +176,73 @@ mg_status ensure_aos(mg_context *ctx) {
 }
 
 mg_status upload_tables(mg_context *ctx) {
-    std::vector<int> fe(ctx->n_full), fo(ctx->n_full);
-    for (int i = 0; i < ctx->n_full; i++) {
+    const int n = ctx->n_full;
+    std::vector<int> fe(n), fo(n);
+    for (int i = 0; i < n; i++) {
         fe[i] = static_cast<int>(ctx->offs.off[0][i]);
         fo[i] = static_cast<int>(ctx->offs.off[1][i]);
     }
-    // reordered lattice tables; site_j - site_i in units of a0/2 = 2 * (vector in units of a0),
-    // small exact integers
+    // gather order (pruned entries first): linear offsets, parity-split index deltas, and the site
+    // vectors in units of a0/2 (2 * the vector in units of a0: small exact integers)
+    std::vector<int> lat[2], lats[2];
     std::vector<float> ds[2];
-    ds[0].resize(3 * ctx->n_full);
-    ds[1].resize(3 * ctx->n_full);
-    std::vector<int> le(ctx->n_full), lo(ctx->n_full);
+    const int64_t half = ctx->g.half;
     for (int p = 0; p < 2; p++) {
-        std::vector<int> &dst = p ? lo : le;
-        for (int q = 0; q < ctx->n_full; q++) {
+        lat[p].resize(n);
+        lats[p].resize(n);
+        ds[p].resize(3 * n);
+        for (int q = 0; q < n; q++) {
             const int e = ctx->lat_order[p][q];
-            dst[q] = static_cast<int>(ctx->offs.off[p][e]);
+            const int64_t o = ctx->offs.off[p][e];
+            lat[p][q] = static_cast<int>(o);
+            // slot s = 2k + p maps to p * half + k; its neighbour s + o has parity p2 and
+            // (s + o) >> 1 = k + floor((p + o) / 2)
+            const int64_t po = p + o;
+            const int64_t p2 = ((po % 2) + 2) % 2;
+            const int64_t fl = po >= 0 ? po / 2 : -((-po + 1) / 2);
+            lats[p][q] = static_cast<int>((p2 - p) * half + fl);
             for (int k = 0; k < 3; k++) ds[p][3 * q + k] = static_cast<float>(2.0 * ctx->offs.vec[p][3 * e + k]);
         }
     }
-    set_constant_tables(fe.data(), fo.data(), ctx->n_full, le.data(), lo.data(), ctx->n_pruned, ds[0].data(),
-                        ds[1].data(), ctx->stream);
+    set_constant_tables(fe.data(), fo.data(), n, lat[0].data(), lat[1].data(), lats[0].data(), lats[1].data(),
+                        ctx->n_pruned, ds[0].data(), ds[1].data(), ctx->stream);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { ctx->err = std::string("constant tables: ") + cudaGetErrorString(e); return MG_ERR_CUDA; }
     return MG_OK;
 }
 
 mg_status install_potential(mg_context *ctx, const HostPotential &hp) {
-    // element tables: double4 value + double4 derivative records, then float4 copies
-    const int ne = hp.n_ele, npair = ne * (ne + 1) / 2;
+    // Tables by atom type (3 x nr / nrho knots) and by type pair (9 x nr, ti * 3 + tj); types whose
+    // element the file lacks point at element 0 and are rejected at upload (types_ok_mask).
+    int ele_of_type[3];
+    ctx->types_ok_mask = 0;
+    for (int t = 0; t < 3; t++) {
+        const int e = hp.ele(type_key(t));
+        if (e >= 0) ctx->types_ok_mask |= 1 << t;
+        ele_of_type[t] = e >= 0 ? e : 0;
+    }
+    if ((hp.nr - 1) * hp.dr + 1e-12 < ctx->g.rc) {  // the hit test uses rc = a0 * cutoff_radius_factor
+        ctx->err = "potential r-table shorter than the cutoff radius";
+        return MG_ERR_POTENTIAL;
+    }
     const size_t nr = hp.nr, nrho = hp.nrho;
-    const size_t n_rec = ne * nrho + ne * nr + npair * nr;  // records per table kind
+    const size_t n_rec = 3 * nr + 3 * nrho + 9 * nr;
     std::vector<Knot64> vd(n_rec), dd(n_rec);
     std::vector<float4> vf(n_rec), df(n_rec);
-    std::vector<size_t> base_F(ne), base_rho(ne), base_z(npair);
     size_t at = 0;
     auto put = [&](const HostSpline &sp) {
-        const size_t b = at;
         for (int m = 0; m < sp.n; m++, at++) {
             vd[at] = Knot64{sp.c0[m], sp.c1[m], sp.c2[m], sp.c3[m]};
             dd[at] = Knot64{sp.d0[m], sp.d1[m], sp.d2[m], 0.0};
             vf[at] = make_float4((float) sp.c0[m], (float) sp.c1[m], (float) sp.c2[m], (float) sp.c3[m]);
             df[at] = make_float4((float) sp.d0[m], (float) sp.d1[m], (float) sp.d2[m], 0.0f);
         }
-        return b;
     };
-    for (int e = 0; e < ne; e++) base_F[e] = put(hp.F[e]);
-    for (int e = 0; e < ne; e++) base_rho[e] = put(hp.rho[e]);
-    for (int q = 0; q < npair; q++) base_z[q] = put(hp.z2[q]);
+    const size_t base_rho = 0, base_F = 3 * nr, base_z = 3 * nr + 3 * nrho;
+    for (int t = 0; t < 3; t++) put(hp.rho[ele_of_type[t]]);
+    for (int t = 0; t < 3; t++) put(hp.F[ele_of_type[t]]);
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) put(hp.z2[HostPotential::pair_index(ele_of_type[a], ele_of_type[b])]);
     if (ctx->pot_mem) { cudaFree(ctx->pot_mem); ctx->pot_mem = nullptr; }
     const size_t bytes = n_rec * (2 * sizeof(Knot64) + 2 * sizeof(float4));
     MG_CK(cudaMalloc(&ctx->pot_mem, bytes));
@@ -244,33 +263,12 @@ mg_status install_potential(mg_context *ctx, const HostPotential &hp) {
     pt.inv_dr_f = (float) pt.inv_dr;
     pt.inv_drho_f = (float) pt.inv_drho;
     pt.h_inv_dr_f = (float) (0.5 * ctx->g.a0 * pt.inv_dr);
-    int ele_of_type[3], pair_of_types[3][3];
-    ctx->types_ok_mask = 0;
-    for (int t = 0; t < 3; t++) {
-        int e = hp.ele(type_key(t));
-        if (e >= 0) ctx->types_ok_mask |= 1 << t;
-        if (e < 0) e = 0;
-        ele_of_type[t] = e;
-    }
-    for (int a = 0; a < 3; a++) {
-        const int ea = ele_of_type[a];
-        pt.F_v[a] = d_vd + base_F[ea]; pt.F_d[a] = d_dd + base_F[ea];
-        pt.rho_v[a] = d_vd + base_rho[ea]; pt.rho_d[a] = d_dd + base_rho[ea];
-        pt.F_vf[a] = d_vf + base_F[ea]; pt.F_df[a] = d_df + base_F[ea];
-        pt.rho_vf[a] = d_vf + base_rho[ea]; pt.rho_df_[a] = d_df + base_rho[ea];
-        for (int b = 0; b < 3; b++) {
-            const int q = HostPotential::pair_index(ea, ele_of_type[b]);
-            pair_of_types[a][b] = q;
-            pt.z_v[a][b] = d_vd + base_z[q]; pt.z_d[a][b] = d_dd + base_z[q];
-            pt.z_vf[a][b] = d_vf + base_z[q]; pt.z_df[a][b] = d_df + base_z[q];
-        }
-    }
-    set_type_maps(ele_of_type, pair_of_types, ctx->stream);
-    // the hit test uses rc = a0 * cutoff_radius_factor; the tables must reach it
-    if ((hp.nr - 1) * hp.dr + 1e-12 < ctx->g.rc) {
-        ctx->err = "potential r-table shorter than the cutoff radius";
-        return MG_ERR_POTENTIAL;
-    }
+    pt.rho_v = d_vd + base_rho; pt.rho_d = d_dd + base_rho;
+    pt.F_v = d_vd + base_F; pt.F_d = d_dd + base_F;
+    pt.z_v = d_vd + base_z; pt.z_d = d_dd + base_z;
+    pt.rho_vf = d_vf + base_rho; pt.rho_dff = d_df + base_rho;
+    pt.F_vf = d_vf + base_F; pt.F_dff = d_df + base_F;
+    pt.z_vf = d_vf + base_z; pt.z_dff = d_df + base_z;
     ctx->hp = hp;
     ctx->pot_ready = true;
     ctx->graph_dt = -1.0;  // rebuild graphs
@@ -358,6 +356,9 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     g.n_slots = (int) (Sx * Sy * Sz);
     g.n_local = g.bx * g.by * g.bz;
     g.n_ghost_slots = g.n_slots - g.n_local;
+    g.half = g.n_slots / 2;  // Sx is even, so slot parity is x parity
+    g.nxh = g.bx / 2;
+    g.n_local_half = g.n_local / 2;
     for (int d = 0; d < 3; d++) g.cells[d] = (int) phase_space[d];
     g.a0 = lattice_const;
     g.rc = lattice_const * rcf;  // atom::atom, src/atom.cpp:14-19

@@ -49,6 +49,9 @@ struct Geom {
     int gx, gy, gz;          // ghost widths (gx doubled)
     int bx, by, bz;          // box sizes (bx doubled)
     int n_slots, n_local, n_ghost_slots;
+    int half;                // n_slots / 2: start of the odd half of the parity-split layout
+    int nxh;                 // bx / 2: sites of one parity per row
+    int n_local_half;        // n_local / 2
     int cells[3];            // phase space in unit cells
     double a0;               // lattice constant (Angstrom)
     double rc, rc2;          // cutoff radius and its square
@@ -68,8 +71,9 @@ struct Slots {
     double *e;               // per-atom energy (energy pass only)
     int8_t *type;
     uint64_t *id;
-    float4 *u4;              // mixed form: displacement from the site in half-lattice units, w = type bits
-    float *df32;             // mixed form: F'(rho) in float
+    // mixed form, parity-split layout (slot s at (s & 1) * half + (s >> 1)):
+    float4 *u4;              // displacement from the site in half-lattice units, w = type bits
+    float *df32;             // F'(rho) in float
 };
 
 // Inter-atom lists (local list in list order; ghost list in receive order).
@@ -107,15 +111,14 @@ struct alignas(32) Knot64 {
 };
 
 // Spline tables on the device. Value records {c0,c1,c2,c3}; derivative records {d0,d1,d2,0}.
+// Laid out by atom type (3 tables of nr or nrho knots) and by type pair (9 tables, ti * 3 + tj),
+// so a lookup is pointer arithmetic on the type, with no per-lane indexed parameter load.
 struct PotTables {
     int nr, nrho;
     double inv_dr, inv_drho;
     float inv_dr_f, inv_drho_f, h_inv_dr_f;   // h_inv_dr_f = (a0/2) / dr
-    // per atom type (0..2): pointers into the element tables
-    const Knot64 *rho_v[3], *rho_d[3], *F_v[3], *F_d[3];
-    const Knot64 *z_v[3][3], *z_d[3][3];
-    const float4 *rho_vf[3], *rho_df_[3], *F_vf[3], *F_df[3];
-    const float4 *z_vf[3][3], *z_df[3][3];
+    const Knot64 *rho_v, *rho_d, *F_v, *F_d, *z_v, *z_d;
+    const float4 *rho_vf, *rho_dff, *F_vf, *F_dff, *z_vf, *z_dff;
 };
 
 // Constant per-step parameters.
@@ -167,9 +170,12 @@ struct LaunchCtx {
     int num_sms;
 };
 
-void set_constant_tables(const int *full_even, const int *full_odd, int n_full, const int *pruned_even,
-                         const int *pruned_odd, int n_pruned, const float *dsite_even, const float *dsite_odd,
-                         cudaStream_t stream);
+// full: reference-order full tables (linear offsets); lat: the gather order (pruned entries first),
+// linear offsets; lats: the same entries as parity-split index deltas; dsite: their site vectors in
+// units of a0/2 (3 floats per entry).
+void set_constant_tables(const int *full_even, const int *full_odd, int n_full, const int *lat_even,
+                         const int *lat_odd, const int *lats_even, const int *lats_odd, int n_pruned,
+                         const float *dsite_even, const float *dsite_odd, cudaStream_t stream);
 
 void launch_unpack_aos(const LaunchCtx &lc, const Geom &g, const mg_atom_element *aos, Slots s, Inter in, int types_ok_mask,
                        bool mixed);
@@ -191,7 +197,6 @@ void launch_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTab
 // far atoms: rebuild the list from positions (uploads, hooks) and the scatter of missed pairs
 void launch_far_rebuild(const LaunchCtx &lc, const Geom &g, Slots s, Inter in);
 void launch_far_scatter(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, int kind, bool mixed);
-void set_type_maps(const int ele_of_type[3], const int pair_of_types[3][3], cudaStream_t stream);
 void launch_inter_manage(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, int steps_mask, bool mixed);
 enum { MANAGE_DECIDE = 1, MANAGE_CLEAR_GHOST = 2, MANAGE_EXCHANGE = 4, MANAGE_BORDER = 8, MANAGE_INDEX = 16 };
 void launch_inter_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed);

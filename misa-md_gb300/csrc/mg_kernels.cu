@@ -22,51 +22,57 @@ namespace mg {
 // ------------------------------------------------------------------------------------------------
 __constant__ int c_full[2][kMaxFull];       // reference full offset tables (linear, per parity)
 __constant__ int c_nfull;
-// Lattice gather table: the full table reordered so that the entries whose sites are closer than
+// Lattice gather tables: the full table reordered so that the entries whose sites are closer than
 // rc + 0.4 a0 come first (c_npruned of them). While every lattice atom is within 0.2 a0 of its site
-// (guaranteed after atom::decide) only those can hold a neighbour inside the cutoff.
-__constant__ int c_pruned[2][kMaxFull];
+// (guaranteed after atom::decide, except for recombined "far" atoms) only those can hold a neighbour
+// inside the cutoff.
+__constant__ int c_lat[2][kMaxFull];        // linear slot offsets
+__constant__ int c_lats[2][kMaxFull];       // parity-split index deltas of the same entries
 __constant__ int c_npruned;
-__constant__ float c_dsite[2][kMaxFull][3];  // site_j - site_i of c_pruned entries, units a0/2
-__constant__ int c_ele_of_type[3];
-__constant__ int c_pair_of_types[3][3];
+__constant__ float4 c_dsite[2][kMaxFull];   // site_j - site_i of the entries, units a0/2 (w unused)
 __constant__ double c_mass[3];
 
-void set_constant_tables(const int *full_even, const int *full_odd, int n_full, const int *pruned_even,
-                         const int *pruned_odd, int n_pruned, const float *dsite_even, const float *dsite_odd,
-                         cudaStream_t stream) {
+void set_constant_tables(const int *full_even, const int *full_odd, int n_full, const int *lat_even,
+                         const int *lat_odd, const int *lats_even, const int *lats_odd, int n_pruned,
+                         const float *dsite_even, const float *dsite_odd, cudaStream_t stream) {
     static int full[2][kMaxFull];
-    static int pruned[2][kMaxFull];
-    static float dsite[2][kMaxFull][3];
-    for (int i = 0; i < n_full; i++) { full[0][i] = full_even[i]; full[1][i] = full_odd[i]; }
+    static int lat[2][kMaxFull];
+    static int lats[2][kMaxFull];
+    static float4 dsite[2][kMaxFull];
     for (int i = 0; i < n_full; i++) {
-        pruned[0][i] = pruned_even[i];
-        pruned[1][i] = pruned_odd[i];
-        for (int k = 0; k < 3; k++) { dsite[0][i][k] = dsite_even[3 * i + k]; dsite[1][i][k] = dsite_odd[3 * i + k]; }
+        full[0][i] = full_even[i]; full[1][i] = full_odd[i];
+        lat[0][i] = lat_even[i]; lat[1][i] = lat_odd[i];
+        lats[0][i] = lats_even[i]; lats[1][i] = lats_odd[i];
+        dsite[0][i] = make_float4(dsite_even[3 * i], dsite_even[3 * i + 1], dsite_even[3 * i + 2], 0.f);
+        dsite[1][i] = make_float4(dsite_odd[3 * i], dsite_odd[3 * i + 1], dsite_odd[3 * i + 2], 0.f);
     }
     const double mass[3] = {atom_mass(0), atom_mass(1), atom_mass(2)};
     cudaMemcpyToSymbolAsync(c_full, full, sizeof(full), 0, cudaMemcpyHostToDevice, stream);
     cudaMemcpyToSymbolAsync(c_nfull, &n_full, sizeof(int), 0, cudaMemcpyHostToDevice, stream);
-    cudaMemcpyToSymbolAsync(c_pruned, pruned, sizeof(pruned), 0, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyToSymbolAsync(c_lat, lat, sizeof(lat), 0, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyToSymbolAsync(c_lats, lats, sizeof(lats), 0, cudaMemcpyHostToDevice, stream);
     cudaMemcpyToSymbolAsync(c_npruned, &n_pruned, sizeof(int), 0, cudaMemcpyHostToDevice, stream);
     cudaMemcpyToSymbolAsync(c_dsite, dsite, sizeof(dsite), 0, cudaMemcpyHostToDevice, stream);
     cudaMemcpyToSymbolAsync(c_mass, mass, sizeof(mass), 0, cudaMemcpyHostToDevice, stream);
     cudaStreamSynchronize(stream);
 }
 
-void set_type_maps(const int ele_of_type[3], const int pair_of_types[3][3], cudaStream_t stream) {
-    static int e[3];
-    static int p[3][3];
-    for (int i = 0; i < 3; i++) { e[i] = ele_of_type[i]; for (int j = 0; j < 3; j++) p[i][j] = pair_of_types[i][j]; }
-    cudaMemcpyToSymbolAsync(c_ele_of_type, e, sizeof(e), 0, cudaMemcpyHostToDevice, stream);
-    cudaMemcpyToSymbolAsync(c_pair_of_types, p, sizeof(p), 0, cudaMemcpyHostToDevice, stream);
-    cudaStreamSynchronize(stream);
-}
 
 // ------------------------------------------------------------------------------------------------
 // index helpers
 // ------------------------------------------------------------------------------------------------
 __device__ __forceinline__ int lin(const Geom &g, int x, int y, int z) { return (z * g.Sy + y) * g.Sx + x; }
+// parity-split index of a slot (x even and odd sites in two halves) for the mixed form's gather arrays
+__device__ __forceinline__ int sidx(const Geom &g, int s) { return (s & 1) * g.half + (s >> 1); }
+// Thread order of the gathers: all even local sites (k, j, i order), then all odd ones, so that a
+// warp has one parity and reads warp-uniform offsets.
+__device__ __forceinline__ int gather_slot(const Geom &g, int t, int &par) {
+    par = t >= g.n_local_half ? 1 : 0;
+    const int u = par ? t - g.n_local_half : t;
+    const int ih = u % g.nxh;
+    const int r = u / g.nxh;
+    return lin(g, 2 * ih + par + g.gx, r % g.by + g.gy, r / g.by + g.gz);
+}
 
 __device__ __forceinline__ int local_slot(const Geom &g, int t, int &i, int &j, int &k) {
     i = t % g.bx;
@@ -234,8 +240,8 @@ __global__ void k_unpack_aos(Geom g, const mg_atom_element *aos, Slots s, Inter 
         const int X = t % g.Sx, r = t / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
         double xs, ys, zs;
         site_of(g, X, Y, Z, xs, ys, zs);
-        s.u4[t] = make_u4(g, a.x[0], a.x[1], a.x[2], xs, ys, zs, a.type);
-        s.df32[t] = (float) a.df;
+        s.u4[sidx(g, t)] = make_u4(g, a.x[0], a.x[1], a.x[2], xs, ys, zs, a.type);
+        s.df32[sidx(g, t)] = (float) a.df;
     }
 }
 
@@ -243,7 +249,7 @@ __global__ void k_pack_aos(Geom g, mg_atom_element *aos, Slots s, int fields, bo
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= g.n_slots) return;
     mg_atom_element &a = aos[t];
-    const double df = mixed ? (double) s.df32[t] : s.df[t];
+    const double df = mixed ? (double) s.df32[sidx(g, t)] : s.df[t];
     if (fields == PACK_ALL) {
         mg_atom_element b;
         b.id = s.id[t];
@@ -309,7 +315,7 @@ __global__ void __launch_bounds__(256) k_firststep(Geom g, Slots s, Inter in, St
     site_of(g, i + g.gx, j + g.gy, k + g.gz, xs, ys, zs);
     const double ex = __dsub_rn(x, xs), ey = __dsub_rn(y, ys), ez = __dsub_rn(z, zs);
     if (MIXED && MOVE) {
-        s.u4[sl] = make_float4(__double2float_rn(__dmul_rn(ex, g.inv_h)), __double2float_rn(__dmul_rn(ey, g.inv_h)),
+        s.u4[sidx(g, sl)] = make_float4(__double2float_rn(__dmul_rn(ex, g.inv_h)), __double2float_rn(__dmul_rn(ey, g.inv_h)),
                                __double2float_rn(__dmul_rn(ez, g.inv_h)), __int_as_float(ty));
     }
     if (DECIDE) {
@@ -405,7 +411,7 @@ __global__ void k_ghost_copy(Geom g, Slots s) {
     s.x[gs] = sx ? __dadd_rn(ox, sx > 0 ? g.L[0] : -g.L[0]) : ox;
     s.y[gs] = sy ? __dadd_rn(oy, sy > 0 ? g.L[1] : -g.L[1]) : oy;
     s.z[gs] = sz ? __dadd_rn(oz, sz > 0 ? g.L[2] : -g.L[2]) : oz;
-    if (MIXED) s.u4[gs] = s.u4[os];
+    if (MIXED) s.u4[sidx(g, gs)] = s.u4[sidx(g, os)];
 }
 void launch_ghost_copy(const LaunchCtx &lc, const Geom &g, Slots s, bool mixed) {
     const int b = 256, n = (g.n_ghost_slots + b - 1) / b;
@@ -420,7 +426,7 @@ __global__ void k_ghost_df(Geom g, Slots s, Inter in) {
     if (t < g.n_ghost_slots) {
         const int gs = ghost_slot(g, t);
         const int os = owner_slot(g, gs);
-        if (MIXED) s.df32[gs] = s.df32[os];
+        if (MIXED) s.df32[sidx(g, gs)] = s.df32[sidx(g, os)];
         else s.df[gs] = s.df[os];
     }
     const int ng = in.cnt[CNT_GHOST];
@@ -434,23 +440,17 @@ void launch_ghost_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool
 
 // ------------------------------------------------------------------------------------------------
 // lattice density pass (atom::latRho, src/atom.cpp:151-192, as a full gather) with dF/drho fused
-// when no inter atom adds density (atom::latDf, src/atom.cpp:286-309).
+// when no inter or far atom adds density afterwards (atom::latDf, src/atom.cpp:286-309).
+// Warps are parity-uniform (gather_slot), so the candidate loop reads warp-uniform constants; far
+// atoms continue over the entries beyond the pruned set.
 // ------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_lat_rho_fp64(Geom g, Slots s, Inter in, PotTables pt, bool hook) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.n_local) return;
-    int i, j, k;
-    const int sl = local_slot(g, t, i, j, k);
-    const int ti = s.type[sl];
-    if (ti < 0) { s.rho[sl] = 0.0; return; }
-    const int par = i & 1;
-    const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
+template <int PAR>
+__device__ __forceinline__ double rho_sum_fp64(const Geom &g, const Slots &s, const PotTables &pt, int sl,
+                                               double xi, double yi, double zi, int q0, int q1) {
     double acc = 0.0;
-    const int np = in.far_flag[sl] ? c_nfull : c_npruned;
 #pragma unroll 4
-    for (int q = 0; q < np; q++) {
-        const int o = par ? c_pruned[1][q] : c_pruned[0][q];
-        const int sj = sl + o;
+    for (int q = q0; q < q1; q++) {
+        const int sj = sl + c_lat[PAR][q];
         const int tj = s.type[sj];
         if (tj < 0) continue;
         const double dx = xi - s.x[sj], dy = yi - s.y[sj], dz = zi - s.z[sj];
@@ -459,54 +459,80 @@ __global__ void __launch_bounds__(256) k_lat_rho_fp64(Geom g, Slots s, Inter in,
             const double r = r2 * rsqrt(r2);
             int m; double p;
             locate_d(r, pt.inv_dr, pt.nr, m, p);
-            acc += val_d(pt.rho_v[tj], m, p);
+            acc += val_d(pt.rho_v + tj * pt.nr, m, p);
         }
+    }
+    return acc;
+}
+
+__global__ void __launch_bounds__(256) k_lat_rho_fp64(Geom g, Slots s, Inter in, PotTables pt, bool hook) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n_local) return;
+    int par;
+    const int sl = gather_slot(g, t, par);
+    const int ti = s.type[sl];
+    if (ti < 0) { s.rho[sl] = 0.0; return; }
+    const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
+    const int np = c_npruned;
+    double acc = par ? rho_sum_fp64<1>(g, s, pt, sl, xi, yi, zi, 0, np) : rho_sum_fp64<0>(g, s, pt, sl, xi, yi, zi, 0, np);
+    if (in.far_flag[sl]) {
+        const int nf = c_nfull;
+        acc += par ? rho_sum_fp64<1>(g, s, pt, sl, xi, yi, zi, np, nf) : rho_sum_fp64<0>(g, s, pt, sl, xi, yi, zi, np, nf);
     }
     s.rho[sl] = acc;
     if (!hook && lattice_only(in)) {
         int m; double p;
         locate_d(acc, pt.inv_drho, pt.nrho, m, p);
-        s.df[sl] = der_d(pt.F_d[ti], m, p);
+        s.df[sl] = der_d(pt.F_d + ti * pt.nrho, m, p);
+    }
+}
+
+template <int PAR>
+__device__ __forceinline__ void rho_sum_mixed(const Geom &g, const Slots &s, const PotTables &pt, int si, float4 ui,
+                                              int q0, int q1, float &sum, float &comp) {
+    const float rc2 = g.rc2_h;
+    const float hinv = pt.h_inv_dr_f;
+#pragma unroll 4
+    for (int q = q0; q < q1; q++) {
+        const float4 uj = __ldg(s.u4 + si + c_lats[PAR][q]);
+        const int tj = __float_as_int(uj.w);
+        if (tj < 0) continue;
+        const float4 D = c_dsite[PAR][q];
+        const float dx = (ui.x - uj.x) - D.x, dy = (ui.y - uj.y) - D.y, dz = (ui.z - uj.z) - D.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 < rc2) {
+            const float rp = r2 * rsqrtf(r2);
+            int m; float p;
+            locate_f(rp, hinv, pt.nr, m, p);
+            kahan(sum, comp, val_f(pt.rho_vf + tj * pt.nr, m, p));
+        }
     }
 }
 
 __global__ void __launch_bounds__(256) k_lat_rho_mixed(Geom g, Slots s, Inter in, PotTables pt, bool hook) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= g.n_local) return;
-    int i, j, k;
-    const int sl = local_slot(g, t, i, j, k);
-    const float4 ui = s.u4[sl];
+    int par;
+    const int sl = gather_slot(g, t, par);
+    const int si = sidx(g, sl);
+    const float4 ui = s.u4[si];
     const int ti = __float_as_int(ui.w);
     if (ti < 0) { s.rho[sl] = 0.0; return; }
-    const int par = i & 1;
     float sum = 0.f, comp = 0.f;
-    const int np = in.far_flag[sl] ? c_nfull : c_npruned;
-    const float rc2 = g.rc2_h;
-    const float hinv = pt.h_inv_dr_f;
-#pragma unroll 4
-    for (int q = 0; q < np; q++) {
-        const int o = par ? c_pruned[1][q] : c_pruned[0][q];
-        const float4 uj = __ldg(s.u4 + sl + o);
-        const int tj = __float_as_int(uj.w);
-        if (tj < 0) continue;
-        const float Dx = par ? c_dsite[1][q][0] : c_dsite[0][q][0];
-        const float Dy = par ? c_dsite[1][q][1] : c_dsite[0][q][1];
-        const float Dz = par ? c_dsite[1][q][2] : c_dsite[0][q][2];
-        const float dx = (ui.x - uj.x) - Dx, dy = (ui.y - uj.y) - Dy, dz = (ui.z - uj.z) - Dz;
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 < rc2) {
-            const float rp = r2 * rsqrtf(r2);
-            int m; float p;
-            locate_f(rp, hinv, pt.nr, m, p);
-            kahan(sum, comp, val_f(pt.rho_vf[tj], m, p));
-        }
+    const int np = c_npruned;
+    if (par) rho_sum_mixed<1>(g, s, pt, si, ui, 0, np, sum, comp);
+    else rho_sum_mixed<0>(g, s, pt, si, ui, 0, np, sum, comp);
+    if (in.far_flag[sl]) {
+        const int nf = c_nfull;
+        if (par) rho_sum_mixed<1>(g, s, pt, si, ui, np, nf, sum, comp);
+        else rho_sum_mixed<0>(g, s, pt, si, ui, np, nf, sum, comp);
     }
     const double rho = (double) sum - (double) comp;
     s.rho[sl] = rho;
     if (!hook && lattice_only(in)) {
         int m; float p;
         locate_f((float) rho, pt.inv_drho_f, pt.nrho, m, p);
-        s.df32[sl] = der_f(pt.F_df[ti], m, p);
+        s.df32[si] = der_f(pt.F_dff + ti * pt.nrho, m, p);
     }
 }
 
@@ -528,11 +554,11 @@ __global__ void k_lat_df(Geom g, Slots s, Inter in, PotTables pt, bool hook) {
         if (MIXED) {
             int m; float p;
             locate_f((float) s.rho[sl], pt.inv_drho_f, pt.nrho, m, p);
-            s.df32[sl] = der_f(pt.F_df[ti], m, p);
+            s.df32[sidx(g, sl)] = der_f(pt.F_dff + ti * pt.nrho, m, p);
         } else {
             int m; double p;
             locate_d(s.rho[sl], pt.inv_drho, pt.nrho, m, p);
-            s.df[sl] = der_d(pt.F_d[ti], m, p);
+            s.df[sl] = der_d(pt.F_d + ti * pt.nrho, m, p);
         }
     }
 }
@@ -544,28 +570,19 @@ void launch_lat_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTab
 }
 
 // ------------------------------------------------------------------------------------------------
-// lattice force pass (atom::latForce, src/atom.cpp:311-358, as a full gather). When no inter atom
-// adds force, the second half-kick (NewtonMotion::secondstep, src/newton_motion.cpp:57-67) is fused.
-// fpair = -(F'_i rho'_j(r) + F'_j rho'_i(r) + phi'_ij(r)) / r, phi = (r phi)/r.
+// lattice force pass (atom::latForce, src/atom.cpp:311-358, as a full gather). When no inter or far
+// atom adds force afterwards, the second half-kick (NewtonMotion::secondstep,
+// src/newton_motion.cpp:57-67) is fused. fpair = -(F'_i rho'_j(r) + F'_j rho'_i(r) + phi'_ij(r)) / r,
+// phi = (r phi) / r.
 // ------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_lat_force_fp64(Geom g, Slots s, Inter in, PotTables pt, StepParams sp,
-                                                        bool kick, bool hook) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.n_local) return;
-    int i, j, k;
-    const int sl = local_slot(g, t, i, j, k);
-    const int ti = s.type[sl];
-    if (ti < 0) { s.fx[sl] = 0.0; s.fy[sl] = 0.0; s.fz[sl] = 0.0; return; }
-    const int par = i & 1;
-    const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
-    const double dfi = s.df[sl];
-    double fx = 0.0, fy = 0.0, fz = 0.0;
-    const int np = in.far_flag[sl] ? c_nfull : c_npruned;
-    const Knot64 *rho_di = pt.rho_d[ti];
+template <int PAR>
+__device__ __forceinline__ void force_sum_fp64(const Geom &g, const Slots &s, const PotTables &pt, int sl, int ti,
+                                               double xi, double yi, double zi, double dfi, int q0, int q1,
+                                               double &fx, double &fy, double &fz) {
+    const Knot64 *rho_di = pt.rho_d + ti * pt.nr;
 #pragma unroll 2
-    for (int q = 0; q < np; q++) {
-        const int o = par ? c_pruned[1][q] : c_pruned[0][q];
-        const int sj = sl + o;
+    for (int q = q0; q < q1; q++) {
+        const int sj = sl + c_lat[PAR][q];
         const int tj = s.type[sj];
         if (tj < 0) continue;
         const double dx = xi - s.x[sj], dy = yi - s.y[sj], dz = zi - s.z[sj];
@@ -575,10 +592,11 @@ __global__ void __launch_bounds__(256) k_lat_force_fp64(Geom g, Slots s, Inter i
             const double r = r2 * rinv;
             int m; double p;
             locate_d(r, pt.inv_dr, pt.nr, m, p);
-            const double rhojp = der_d(pt.rho_d[tj], m, p);
+            const double rhojp = der_d(pt.rho_d + tj * pt.nr, m, p);
             const double rhoip = (tj == ti) ? rhojp : der_d(rho_di, m, p);
-            const double zv = val_d(pt.z_v[ti][tj], m, p);
-            const double zp = der_d(pt.z_d[ti][tj], m, p);
+            const int pr = (ti * 3 + tj) * pt.nr;
+            const double zv = val_d(pt.z_v + pr, m, p);
+            const double zp = der_d(pt.z_d + pr, m, p);
             const double phi = zv * rinv;
             const double phip = zp * rinv - phi * rinv;
             const double psip = dfi * rhojp + s.df[sj] * rhoip + phip;
@@ -587,6 +605,27 @@ __global__ void __launch_bounds__(256) k_lat_force_fp64(Geom g, Slots s, Inter i
             fy += dy * fpair;
             fz += dz * fpair;
         }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_lat_force_fp64(Geom g, Slots s, Inter in, PotTables pt, StepParams sp,
+                                                        bool kick, bool hook) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n_local) return;
+    int par;
+    const int sl = gather_slot(g, t, par);
+    const int ti = s.type[sl];
+    if (ti < 0) { s.fx[sl] = 0.0; s.fy[sl] = 0.0; s.fz[sl] = 0.0; return; }
+    const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
+    const double dfi = s.df[sl];
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    const int np = c_npruned;
+    if (par) force_sum_fp64<1>(g, s, pt, sl, ti, xi, yi, zi, dfi, 0, np, fx, fy, fz);
+    else force_sum_fp64<0>(g, s, pt, sl, ti, xi, yi, zi, dfi, 0, np, fx, fy, fz);
+    if (in.far_flag[sl]) {
+        const int nf = c_nfull;
+        if (par) force_sum_fp64<1>(g, s, pt, sl, ti, xi, yi, zi, dfi, np, nf, fx, fy, fz);
+        else force_sum_fp64<0>(g, s, pt, sl, ti, xi, yi, zi, dfi, np, nf, fx, fy, fz);
     }
     s.fx[sl] = fx; s.fy[sl] = fy; s.fz[sl] = fz;
     if (kick && !hook && lattice_only(in)) {
@@ -597,57 +636,68 @@ __global__ void __launch_bounds__(256) k_lat_force_fp64(Geom g, Slots s, Inter i
     }
 }
 
-__global__ void __launch_bounds__(256) k_lat_force_mixed(Geom g, Slots s, Inter in, PotTables pt, StepParams sp,
-                                                         bool kick, bool hook) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.n_local) return;
-    int i, j, k;
-    const int sl = local_slot(g, t, i, j, k);
-    const float4 ui = s.u4[sl];
-    const int ti = __float_as_int(ui.w);
-    if (ti < 0) { s.fx[sl] = 0.0; s.fy[sl] = 0.0; s.fz[sl] = 0.0; return; }
-    const int par = i & 1;
-    const float dfi = s.df32[sl];
-    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-    const int np = in.far_flag[sl] ? c_nfull : c_npruned;
+template <int PAR>
+__device__ __forceinline__ void force_sum_mixed(const Geom &g, const Slots &s, const PotTables &pt, int si, int ti,
+                                                float4 ui, float dfi, int q0, int q1, float acc[6]) {
     const float rc2 = g.rc2_h;
     const float hinv = pt.h_inv_dr_f;
     const float inv_h = 1.0f / g.h_f;
-    const float4 *rho_di = pt.rho_df_[ti];
+    const float4 *rho_di = pt.rho_dff + ti * pt.nr;
 #pragma unroll 2
-    for (int q = 0; q < np; q++) {
-        const int o = par ? c_pruned[1][q] : c_pruned[0][q];
-        const float4 uj = __ldg(s.u4 + sl + o);
+    for (int q = q0; q < q1; q++) {
+        const int oj = si + c_lats[PAR][q];
+        const float4 uj = __ldg(s.u4 + oj);
         const int tj = __float_as_int(uj.w);
         if (tj < 0) continue;
-        const float Dx = par ? c_dsite[1][q][0] : c_dsite[0][q][0];
-        const float Dy = par ? c_dsite[1][q][1] : c_dsite[0][q][1];
-        const float Dz = par ? c_dsite[1][q][2] : c_dsite[0][q][2];
-        const float dx = (ui.x - uj.x) - Dx, dy = (ui.y - uj.y) - Dy, dz = (ui.z - uj.z) - Dz;
+        const float4 D = c_dsite[PAR][q];
+        const float dx = (ui.x - uj.x) - D.x, dy = (ui.y - uj.y) - D.y, dz = (ui.z - uj.z) - D.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (r2 < rc2) {
             const float rinv_h = rsqrtf(r2);
             const float rp = r2 * rinv_h;
             int m; float p;
             locate_f(rp, hinv, pt.nr, m, p);
-            const float rhojp = der_f(pt.rho_df_[tj], m, p);
+            const float rhojp = der_f(pt.rho_dff + tj * pt.nr, m, p);
             const float rhoip = (tj == ti) ? rhojp : der_f(rho_di, m, p);
-            const float zv = val_f(pt.z_vf[ti][tj], m, p);
-            const float zp = der_f(pt.z_df[ti][tj], m, p);
+            const int pr = (ti * 3 + tj) * pt.nr;
+            const float zv = val_f(pt.z_vf + pr, m, p);
+            const float zp = der_f(pt.z_dff + pr, m, p);
             const float rinv = rinv_h * inv_h;
             const float phi = zv * rinv;
             const float phip = zp * rinv - phi * rinv;
-            const float psip = dfi * rhojp + __ldg(s.df32 + sl + o) * rhoip + phip;
+            const float psip = dfi * rhojp + __ldg(s.df32 + oj) * rhoip + phip;
             const float fpair = -psip * rinv;
-            kahan(sx, cx, dx * fpair);
-            kahan(sy, cy, dy * fpair);
-            kahan(sz, cz, dz * fpair);
+            kahan(acc[0], acc[3], dx * fpair);
+            kahan(acc[1], acc[4], dy * fpair);
+            kahan(acc[2], acc[5], dz * fpair);
         }
     }
+}
+
+__global__ void __launch_bounds__(256) k_lat_force_mixed(Geom g, Slots s, Inter in, PotTables pt, StepParams sp,
+                                                         bool kick, bool hook) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n_local) return;
+    int par;
+    const int sl = gather_slot(g, t, par);
+    const int si = sidx(g, sl);
+    const float4 ui = s.u4[si];
+    const int ti = __float_as_int(ui.w);
+    if (ti < 0) { s.fx[sl] = 0.0; s.fy[sl] = 0.0; s.fz[sl] = 0.0; return; }
+    const float dfi = s.df32[si];
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // sums x, y, z and their Kahan compensations
+    const int np = c_npruned;
+    if (par) force_sum_mixed<1>(g, s, pt, si, ti, ui, dfi, 0, np, acc);
+    else force_sum_mixed<0>(g, s, pt, si, ti, ui, dfi, 0, np, acc);
+    if (in.far_flag[sl]) {
+        const int nf = c_nfull;
+        if (par) force_sum_mixed<1>(g, s, pt, si, ti, ui, dfi, np, nf, acc);
+        else force_sum_mixed<0>(g, s, pt, si, ti, ui, dfi, np, nf, acc);
+    }
     const double h = 0.5 * g.a0;
-    const double fx = h * ((double) sx - (double) cx);
-    const double fy = h * ((double) sy - (double) cy);
-    const double fz = h * ((double) sz - (double) cz);
+    const double fx = h * ((double) acc[0] - (double) acc[3]);
+    const double fy = h * ((double) acc[1] - (double) acc[4]);
+    const double fz = h * ((double) acc[2] - (double) acc[5]);
     s.fx[sl] = fx; s.fy[sl] = fy; s.fz[sl] = fz;
     if (kick && !hook && lattice_only(in)) {
         const double c = dt_inv_m_of(sp, ti);
@@ -697,57 +747,75 @@ void launch_secondstep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, St
 // ------------------------------------------------------------------------------------------------
 // per-atom energy (extension): e_i = F(rho_i) + 1/2 sum_j phi_ij over lattice neighbours
 // ------------------------------------------------------------------------------------------------
+template <int PAR>
+__device__ __forceinline__ double energy_sum_fp64(const Geom &g, const Slots &s, const PotTables &pt, int sl, int ti,
+                                                  int q0, int q1) {
+    const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
+    double acc = 0.0;
+    for (int q = q0; q < q1; q++) {
+        const int sj = sl + c_lat[PAR][q];
+        const int tj = s.type[sj];
+        if (tj < 0) continue;
+        const double dx = xi - s.x[sj], dy = yi - s.y[sj], dz = zi - s.z[sj];
+        const double r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 < g.rc2) {
+            const double rinv = rsqrt(r2);
+            int m; double p;
+            locate_d(r2 * rinv, pt.inv_dr, pt.nr, m, p);
+            acc += val_d(pt.z_v + (ti * 3 + tj) * pt.nr, m, p) * rinv;
+        }
+    }
+    return acc;
+}
+template <int PAR>
+__device__ __forceinline__ void energy_sum_mixed(const Geom &g, const Slots &s, const PotTables &pt, int si, int ti,
+                                                 float4 ui, int q0, int q1, float &sum, float &comp) {
+    const float inv_h = 1.0f / g.h_f;
+    for (int q = q0; q < q1; q++) {
+        const float4 uj = __ldg(s.u4 + si + c_lats[PAR][q]);
+        const int tj = __float_as_int(uj.w);
+        if (tj < 0) continue;
+        const float4 D = c_dsite[PAR][q];
+        const float dx = (ui.x - uj.x) - D.x, dy = (ui.y - uj.y) - D.y, dz = (ui.z - uj.z) - D.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 < g.rc2_h) {
+            const float rinv_h = rsqrtf(r2);
+            int m; float p;
+            locate_f(r2 * rinv_h, pt.h_inv_dr_f, pt.nr, m, p);
+            kahan(sum, comp, val_f(pt.z_vf + (ti * 3 + tj) * pt.nr, m, p) * (rinv_h * inv_h));
+        }
+    }
+}
+
 template <bool MIXED>
 __global__ void __launch_bounds__(256) k_energy(Geom g, Slots s, Inter in, PotTables pt) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= g.n_local) return;
-    int i, j, k;
-    const int sl = local_slot(g, t, i, j, k);
+    int par;
+    const int sl = gather_slot(g, t, par);
     const int ti = s.type[sl];
     if (ti < 0) { s.e[sl] = 0.0; return; }
-    const int par = i & 1;
-    const int np = in.far_flag[sl] ? c_nfull : c_npruned;
+    const int np = c_npruned;
+    const int nq = in.far_flag[sl] ? c_nfull : np;
     if (!MIXED) {
-        const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
-        double acc = 0.0;
-        for (int q = 0; q < np; q++) {
-            const int sj = sl + (par ? c_pruned[1][q] : c_pruned[0][q]);
-            const int tj = s.type[sj];
-            if (tj < 0) continue;
-            const double dx = xi - s.x[sj], dy = yi - s.y[sj], dz = zi - s.z[sj];
-            const double r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < g.rc2) {
-                const double rinv = rsqrt(r2);
-                int m; double p;
-                locate_d(r2 * rinv, pt.inv_dr, pt.nr, m, p);
-                acc += val_d(pt.z_v[ti][tj], m, p) * rinv;
-            }
-        }
+        double acc = par ? energy_sum_fp64<1>(g, s, pt, sl, ti, 0, np) : energy_sum_fp64<0>(g, s, pt, sl, ti, 0, np);
+        if (nq > np) acc += par ? energy_sum_fp64<1>(g, s, pt, sl, ti, np, nq) : energy_sum_fp64<0>(g, s, pt, sl, ti, np, nq);
         int m; double p;
         locate_d(s.rho[sl], pt.inv_drho, pt.nrho, m, p);
-        s.e[sl] = val_d(pt.F_v[ti], m, p) + 0.5 * acc;
+        s.e[sl] = val_d(pt.F_v + ti * pt.nrho, m, p) + 0.5 * acc;
     } else {
-        const float4 ui = s.u4[sl];
+        const int si = sidx(g, sl);
+        const float4 ui = s.u4[si];
         float sum = 0.f, comp = 0.f;
-        const float inv_h = 1.0f / g.h_f;
-        for (int q = 0; q < np; q++) {
-            const float4 uj = __ldg(s.u4 + sl + (par ? c_pruned[1][q] : c_pruned[0][q]));
-            const int tj = __float_as_int(uj.w);
-            if (tj < 0) continue;
-            const float dx = (ui.x - uj.x) - (par ? c_dsite[1][q][0] : c_dsite[0][q][0]);
-            const float dy = (ui.y - uj.y) - (par ? c_dsite[1][q][1] : c_dsite[0][q][1]);
-            const float dz = (ui.z - uj.z) - (par ? c_dsite[1][q][2] : c_dsite[0][q][2]);
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < g.rc2_h) {
-                const float rinv_h = rsqrtf(r2);
-                int m; float p;
-                locate_f(r2 * rinv_h, pt.h_inv_dr_f, pt.nr, m, p);
-                kahan(sum, comp, val_f(pt.z_vf[ti][tj], m, p) * (rinv_h * inv_h));
-            }
+        if (par) energy_sum_mixed<1>(g, s, pt, si, ti, ui, 0, np, sum, comp);
+        else energy_sum_mixed<0>(g, s, pt, si, ti, ui, 0, np, sum, comp);
+        if (nq > np) {
+            if (par) energy_sum_mixed<1>(g, s, pt, si, ti, ui, np, nq, sum, comp);
+            else energy_sum_mixed<0>(g, s, pt, si, ti, ui, np, nq, sum, comp);
         }
         int m; float p;
         locate_f((float) s.rho[sl], pt.inv_drho_f, pt.nrho, m, p);
-        s.e[sl] = (double) val_f(pt.F_vf[ti], m, p) + 0.5 * ((double) sum - (double) comp);
+        s.e[sl] = (double) val_f(pt.F_vf + ti * pt.nrho, m, p) + 0.5 * ((double) sum - (double) comp);
     }
 }
 void launch_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
@@ -877,10 +945,10 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s
                 in.vx[a] = s.vx[sl]; in.vy[a] = s.vy[sl]; in.vz[a] = s.vz[sl];
                 in.fx[a] = s.fx[sl]; in.fy[a] = s.fy[sl]; in.fz[a] = s.fz[sl];
                 in.rho[a] = s.rho[sl];
-                in.df[a] = mixed ? (double) s.df32[sl] : s.df[sl];
+                in.df[a] = mixed ? (double) s.df32[sidx(g, sl)] : s.df[sl];
                 s.type[sl] = kInvalid;
                 s.vx[sl] = 0.0; s.vy[sl] = 0.0; s.vz[sl] = 0.0;
-                if (mixed) { float4 u = s.u4[sl]; u.w = __int_as_float(kInvalid); s.u4[sl] = u; }
+                if (mixed) { float4 u = s.u4[sidx(g, sl)]; u.w = __int_as_float(kInvalid); s.u4[sidx(g, sl)] = u; }
             }
             __syncthreads();
             if (tid == 0) in.cnt[CNT_INTER] = n0 + nd;
@@ -916,7 +984,7 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s
                 const int X = sl % g.Sx, r = sl / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
                 double xs, ys, zs;
                 site_of(g, X, Y, Z, xs, ys, zs);
-                s.u4[sl] = make_u4(g, in.x[a], in.y[a], in.z[a], xs, ys, zs, in.type[a]);
+                s.u4[sidx(g, sl)] = make_u4(g, in.x[a], in.y[a], in.z[a], xs, ys, zs, in.type[a]);
             }
             // a recombined atom may sit up to sqrt(5)/4 a0 from its new site
             if (displaced_fp64(g, s, sl)) {
@@ -1091,16 +1159,16 @@ __device__ __forceinline__ InterRef inter_ref(const Inter &in, int ref) {
 __device__ __forceinline__ double rho_fn(const PotTables &pt, int type, double r2) {
     int m; double p;
     locate_d(sqrt(r2), pt.inv_dr, pt.nr, m, p);
-    return val_d(pt.rho_v[type], m, p);
+    return val_d(pt.rho_v + type * pt.nr, m, p);
 }
 __device__ __forceinline__ double to_force(const PotTables &pt, int ti, int tj, double r2, double dfi, double dfj) {
     const double r = sqrt(r2);
     int m; double p;
     locate_d(r, pt.inv_dr, pt.nr, m, p);
-    const double rhoip = der_d(pt.rho_d[ti], m, p);
-    const double rhojp = der_d(pt.rho_d[tj], m, p);
-    const double zv = val_d(pt.z_v[ti][tj], m, p);
-    const double zp = der_d(pt.z_d[ti][tj], m, p);
+    const double rhoip = der_d(pt.rho_d + ti * pt.nr, m, p);
+    const double rhojp = der_d(pt.rho_d + tj * pt.nr, m, p);
+    const double zv = val_d(pt.z_v + (ti * 3 + tj) * pt.nr, m, p);
+    const double zp = der_d(pt.z_d + (ti * 3 + tj) * pt.nr, m, p);
     const double recip = 1.0 / r;
     const double phi = zv * recip;
     const double phip = zp * recip - phi * recip;
@@ -1111,9 +1179,11 @@ __device__ __forceinline__ double pair_fn(const PotTables &pt, int ti, int tj, d
     const double r = sqrt(r2);
     int m; double p;
     locate_d(r, pt.inv_dr, pt.nr, m, p);
-    return val_d(pt.z_v[ti][tj], m, p) / r;
+    return val_d(pt.z_v + (ti * 3 + tj) * pt.nr, m, p) / r;
 }
-__device__ __forceinline__ double lat_df(const Slots &s, int sl, bool mixed) { return mixed ? (double) s.df32[sl] : s.df[sl]; }
+__device__ __forceinline__ double lat_df(const Geom &g, const Slots &s, int sl, bool mixed) {
+    return mixed ? (double) s.df32[sidx(g, sl)] : s.df[sl];
+}
 
 // kind: 0 density, 1 force, 2 energy
 template <int KIND>
@@ -1144,7 +1214,7 @@ __global__ void k_inter_eam(Geom g, Slots s, Inter in, PotTables pt, bool mixed)
                 acc += rho_fn(pt, tj, r2);
                 atomicAdd(&s.rho[own], rho_fn(pt, ta, r2));
             } else if (KIND == 1) {
-                const double fp = to_force(pt, ta, tj, r2, dfa, lat_df(s, sj, mixed));
+                const double fp = to_force(pt, ta, tj, r2, dfa, lat_df(g, s, sj, mixed));
                 fx += dx * fp; fy += dy * fp; fz += dz * fp;
                 atomicAdd(&s.fx[own], -dx * fp);
                 atomicAdd(&s.fy[own], -dy * fp);
@@ -1177,13 +1247,13 @@ __global__ void k_inter_eam(Geom g, Slots s, Inter in, PotTables pt, bool mixed)
             in.rho[a] = acc;
             int m; double p;
             locate_d(acc, pt.inv_drho, pt.nrho, m, p);
-            in.df[a] = der_d(pt.F_d[ta], m, p);
+            in.df[a] = der_d(pt.F_d + ta * pt.nrho, m, p);
         } else if (KIND == 1) {
             in.fx[a] = fx; in.fy[a] = fy; in.fz[a] = fz;
         } else {
             int m; double p;
             locate_d(in.rho[a], pt.inv_drho, pt.nrho, m, p);
-            in.e[a] = val_d(pt.F_v[ta], m, p) + acc;
+            in.e[a] = val_d(pt.F_v + ta * pt.nrho, m, p) + acc;
         }
     }
 }
@@ -1238,9 +1308,9 @@ __global__ void k_far_scatter(Geom g, Slots s, Inter in, PotTables pt, bool mixe
         if (ti < 0) continue;
         const int par = (sl % g.Sx) & 1;
         const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
-        const double dfi = mixed ? (double) s.df32[sl] : s.df[sl];
+        const double dfi = lat_df(g, s, sl, mixed);
         for (int q = np; q < nfull; q++) {
-            const int sj = sl + (par ? c_pruned[1][q] : c_pruned[0][q]);
+            const int sj = sl + (par ? c_lat[1][q] : c_lat[0][q]);
             const int tj = s.type[sj];
             if (tj < 0) continue;
             const int own = owner_slot(g, sj);
@@ -1252,11 +1322,11 @@ __global__ void k_far_scatter(Geom g, Slots s, Inter in, PotTables pt, bool mixe
             int m; double p;
             locate_d(r, pt.inv_dr, pt.nr, m, p);
             if (KIND == 0) {
-                atomicAdd(&s.rho[own], val_d(pt.rho_v[ti], m, p));
+                atomicAdd(&s.rho[own], val_d(pt.rho_v + ti * pt.nr, m, p));
             } else if (KIND == 1) {
-                const double dfj = mixed ? (double) s.df32[sj] : s.df[sj];
-                const double rhoip = der_d(pt.rho_d[ti], m, p), rhojp = der_d(pt.rho_d[tj], m, p);
-                const double zv = val_d(pt.z_v[ti][tj], m, p), zp = der_d(pt.z_d[ti][tj], m, p);
+                const double dfj = lat_df(g, s, sj, mixed);
+                const double rhoip = der_d(pt.rho_d + ti * pt.nr, m, p), rhojp = der_d(pt.rho_d + tj * pt.nr, m, p);
+                const double zv = val_d(pt.z_v + (ti * 3 + tj) * pt.nr, m, p), zp = der_d(pt.z_d + (ti * 3 + tj) * pt.nr, m, p);
                 const double recip = 1.0 / r;
                 const double phi = zv * recip;
                 const double phip = zp * recip - phi * recip;
@@ -1265,7 +1335,7 @@ __global__ void k_far_scatter(Geom g, Slots s, Inter in, PotTables pt, bool mixe
                 atomicAdd(&s.fy[own], -dy * fp);
                 atomicAdd(&s.fz[own], -dz * fp);
             } else {
-                atomicAdd(&s.e[own], 0.5 * val_d(pt.z_v[ti][tj], m, p) / r);
+                atomicAdd(&s.e[own], 0.5 * val_d(pt.z_v + (ti * 3 + tj) * pt.nr, m, p) / r);
             }
         }
     }
