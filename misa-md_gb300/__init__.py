@@ -91,6 +91,7 @@ _PROTOS = {
     "mg_stream": (_P, [_P]),
     "mg_host_register": (_I32, [_P, _U64]),
     "mg_host_unregister": (_I32, [_P]),
+    "mg_mvv_noalloc": (_I32, [_P, _P, _P, _P, _I64, _P, _P]),
 }
 
 

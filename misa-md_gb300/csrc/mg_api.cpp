@@ -23,6 +23,11 @@ const char *kTimerNames[kNumTimers] = {"firststep", "inter_firststep", "inter_ma
 
 }  // namespace
 
+namespace mg {
+// message returned by mg_last_error(NULL) (entry points that take no context)
+void set_global_error(const char *msg) { g_create_error = msg ? msg : ""; }
+}  // namespace mg
+
 struct mg_context {
     int device = 0;
     int precision = MG_PREC_FP64;
