@@ -237,12 +237,15 @@ def run_ours(args):
     gen_s = time.perf_counter() - t0
     n_atoms = w.n_atoms
 
+    tuning = {}
+
     def make_ctx(prec):
         c = pkg.Context(w.cells, w.lattice_const, w.cutoff_radius_factor, precision=prec, device=local_rank)
         c.pot_init_setfl(pot)
         c.set_timestep(w.dt)
         c.upload(atoms)
         c.prepare()
+        tuning[prec] = c.autotune(reps=2)  # cached per (box, precision) after the first call
         return c
 
     # ---- resident ----
@@ -280,7 +283,8 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                               "ms_per_step": ms_per_step, "precision": args.precision, "workload": w.name,
-                              "kernel_ms_per_step": kt, "roofline_achieved_gbs": achieved, "clocks": clocks}))
+                              "kernel_ms_per_step": kt, "roofline_achieved_gbs": achieved, "clocks": clocks,
+                              "tuning": tuning}))
         return
 
     # ---- accuracy of the mixed form against the FP64 form on the same state ----
@@ -371,6 +375,7 @@ def run_ours(args):
         "accuracy": {"force_rms_ev_per_A": f_rms, "force_max_ev_per_A": f_max, "reference": "FP64 GPU form",
                      "nve_drift": drift},
         "gpu_launches": launches,
+        "tuning": tuning,
         "clocks": clocks,
         "state": {"n_inter": thermo["n_inter"], "device_errors": thermo["device_errors"], "gen_s": gen_s},
     }

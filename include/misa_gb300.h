@@ -187,6 +187,15 @@ mg_status mg_step_host(mg_context *ctx, mg_atom_element *atoms, int64_t n_slots,
 mg_status mg_ws_map(mg_context *ctx, const double *xyz, int64_t n, int64_t *coords, uint32_t *flags,
                     int64_t *index);
 
+/* Autotuner: times the density and force passes of the current precision on the resident state for
+ * every gather thread order (0: all even sites then all odd; 1: even/odd warps interleaved per 32
+ * sites) and block size (128, 256, 512), reps launches each, and keeps the fastest. Results are cached
+ * per (box, precision) for the life of the process. out (may be NULL) receives {rho order, rho block,
+ * force order, force block}. Needs mg_prepare first. */
+mg_status mg_autotune(mg_context *ctx, int32_t reps, int32_t out[4]);
+/* Sets the four tuning values directly (same layout as mg_autotune's out). */
+mg_status mg_set_tuning(mg_context *ctx, const int32_t tune[4]);
+
 /* Measured kernel times of the last mg_simulate call with timing enabled (ms per step per kernel). */
 mg_status mg_enable_timing(mg_context *ctx, int32_t on);
 mg_status mg_kernel_times(const mg_context *ctx, double *ms, int32_t cap, int32_t *n, const char **names);

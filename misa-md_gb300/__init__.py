@@ -92,6 +92,8 @@ _PROTOS = {
     "mg_host_register": (_I32, [_P, _U64]),
     "mg_host_unregister": (_I32, [_P]),
     "mg_mvv_noalloc": (_I32, [_P, _P, _P, _P, _I64, _P, _P]),
+    "mg_autotune": (_I32, [_P, _I32, _P]),
+    "mg_set_tuning": (_I32, [_P, _P]),
 }
 
 
@@ -305,6 +307,16 @@ class Context:
         index = np.zeros(n, dtype=np.int64)
         self._check(self.lib.mg_ws_map(self.h, _ptr(xyz), n, _ptr(coords), _ptr(flags), _ptr(index)))
         return coords, flags, index
+
+    def autotune(self, reps=3):
+        out = np.zeros(4, dtype=np.int32)
+        self._check(self.lib.mg_autotune(self.h, int(reps), _ptr(out)))
+        return {"rho_order": int(out[0]), "rho_block": int(out[1]), "force_order": int(out[2]),
+                "force_block": int(out[3])}
+
+    def set_tuning(self, rho_order, rho_block, force_order, force_block):
+        t = np.asarray([rho_order, rho_block, force_order, force_block], dtype=np.int32)
+        self._check(self.lib.mg_set_tuning(self.h, _ptr(t)))
 
     def enable_timing(self, on=True):
         self._check(self.lib.mg_enable_timing(self.h, 1 if on else 0))

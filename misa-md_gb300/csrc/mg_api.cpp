@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <array>
 #include <vector>
 
 #include "mg_internal.h"
@@ -67,7 +68,15 @@ struct mg_context {
     int64_t timed_steps = 0;
     bool energy_valid = false;
 
-    LaunchCtx lc() const { return LaunchCtx{stream, num_sms}; }
+    int tune[2][2][2] = {{{0, 256}, {0, 256}}, {{0, 256}, {0, 256}}};  // [precision][rho, force] = {order, block}
+    LaunchCtx lc() const {
+        LaunchCtx l{stream, num_sms};
+        l.rho_order = tune[precision][0][0];
+        l.rho_block = tune[precision][0][1];
+        l.force_order = tune[precision][1][0];
+        l.force_block = tune[precision][1][1];
+        return l;
+    }
     bool mixed() const { return precision == MG_PREC_MIXED; }
 };
 
@@ -146,7 +155,6 @@ void seq_compute_eam(mg_context *ctx, bool kick, bool with_manage_prefix, int ma
     if (t) t->mark(4);
     launch_lat_rho(lc, ctx->g, ctx->s, ctx->in, ctx->pt, mx, false);
     if (t) t->mark(5);
-    launch_far_scatter(lc, ctx->g, ctx->s, ctx->in, ctx->pt, 0, mx);
     launch_inter_rho(lc, ctx->g, ctx->s, ctx->in, ctx->pt, mx);
     if (t) t->mark(6);
     launch_lat_df(lc, ctx->g, ctx->s, ctx->in, ctx->pt, mx, false);
@@ -155,7 +163,6 @@ void seq_compute_eam(mg_context *ctx, bool kick, bool with_manage_prefix, int ma
     if (t) t->mark(8);
     launch_lat_force(lc, ctx->g, ctx->s, ctx->in, ctx->pt, ctx->sp, kick, mx, false);
     if (t) t->mark(9);
-    launch_far_scatter(lc, ctx->g, ctx->s, ctx->in, ctx->pt, 1, mx);
     launch_inter_force(lc, ctx->g, ctx->s, ctx->in, ctx->pt, mx);
     if (t) t->mark(10);
     if (kick) launch_secondstep(lc, ctx->g, ctx->s, ctx->in, ctx->sp, false);
@@ -372,6 +379,8 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     for (int d = 0; d < 3; d++) g.L[d] = phase_space[d] * lattice_const;
     g.inv_h = 2.0 / lattice_const;
     g.h_f = (float) (0.5 * lattice_const);
+    g.inv_h_f = (float) g.inv_h;
+    g.thr_lo_f = (float) (g.thr * (1.0 - 1e-4));
     g.rc2_h = (float) (g.rc2 * g.inv_h * g.inv_h);
 
     // offset tables, and the lattice gather order: pruned entries (site distance below
@@ -567,7 +576,6 @@ mg_status mg_eam_rho_calc(mg_context *ctx, mg_atom_element *atoms, double cutoff
     mg_status st = hook_upload(ctx, atoms, cutoff_radius);
     if (st != MG_OK) return st;
     launch_lat_rho(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, ctx->mixed(), true);
-    launch_far_scatter(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, 0, ctx->mixed());
     return hook_download(ctx, atoms, PACK_RHO);
 }
 mg_status mg_eam_df_calc(mg_context *ctx, mg_atom_element *atoms, double cutoff_radius) {
@@ -581,7 +589,6 @@ mg_status mg_eam_force_calc(mg_context *ctx, mg_atom_element *atoms, double cuto
     if (st != MG_OK) return st;
     StepParams none{};
     launch_lat_force(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, none, false, ctx->mixed(), true);
-    launch_far_scatter(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, 1, ctx->mixed());
     return hook_download(ctx, atoms, PACK_F);
 }
 
@@ -812,7 +819,6 @@ mg_status mg_thermo(mg_context *ctx, int32_t with_energy, mg_thermo_out *out) {
     if (with_energy) {
         if ((st = require_ready(ctx)) != MG_OK) return st;
         launch_energy(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, ctx->mixed());
-        launch_far_scatter(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, 2, ctx->mixed());
         launch_inter_energy(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, ctx->mixed());
         ctx->energy_valid = true;
     }
@@ -893,6 +899,84 @@ mg_status mg_ws_map(mg_context *ctx, const double *xyz, int64_t n, int64_t *coor
     MG_CK(cudaMemcpyAsync(flags, ctx->d_ws_flags, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     MG_CK(cudaMemcpyAsync(index, ctx->d_ws_index, n * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
     MG_CK(cudaStreamSynchronize(ctx->stream));
+    return MG_OK;
+}
+
+// Autotuner: times each gather kernel of the current precision for every (thread order, block size)
+// on the resident state and keeps the fastest; results are cached per (box, precision) for the process.
+namespace {
+struct TuneKey {
+    int cells[3], precision;
+    bool operator==(const TuneKey &o) const {
+        return cells[0] == o.cells[0] && cells[1] == o.cells[1] && cells[2] == o.cells[2] && precision == o.precision;
+    }
+};
+std::vector<std::pair<TuneKey, std::array<int, 4>>> g_tune_cache;
+}  // namespace
+
+mg_status mg_autotune(mg_context *ctx, int32_t reps, int32_t out[4]) {
+    if (!ctx) return MG_ERR_ARG;
+    if (!ctx->prepared) { ctx->err = "mg_prepare must run before mg_autotune"; return MG_ERR_STATE; }
+    const int p = ctx->precision;
+    const TuneKey key{{ctx->g.cells[0], ctx->g.cells[1], ctx->g.cells[2]}, p};
+    for (auto &kv : g_tune_cache) {
+        if (kv.first == key) {
+            for (int k = 0; k < 2; k++) { ctx->tune[p][k][0] = kv.second[2 * k]; ctx->tune[p][k][1] = kv.second[2 * k + 1]; }
+            if (out) for (int k = 0; k < 4; k++) out[k] = kv.second[k];
+            ctx->graph_dt = -1.0;
+            return MG_OK;
+        }
+    }
+    if (reps < 1) reps = 3;
+    cudaEvent_t e0, e1;
+    MG_CK(cudaEventCreate(&e0));
+    MG_CK(cudaEventCreate(&e1));
+    const int blocks[3] = {128, 256, 512};
+    std::array<int, 4> best{};
+    StepParams none{};
+    for (int kern = 0; kern < 2; kern++) {
+        float best_ms = 1e30f;
+        for (int order = 0; order < 2; order++) {
+            for (int b : blocks) {
+                ctx->tune[p][kern][0] = order;
+                ctx->tune[p][kern][1] = b;
+                const LaunchCtx lc = ctx->lc();
+                auto run = [&]() {
+                    if (kern == 0) launch_lat_rho(lc, ctx->g, ctx->s, ctx->in, ctx->pt, ctx->mixed(), false);
+                    else launch_lat_force(lc, ctx->g, ctx->s, ctx->in, ctx->pt, none, false, ctx->mixed(), false);
+                };
+                run();  // warm
+                cudaEventRecord(e0, ctx->stream);
+                for (int r = 0; r < reps; r++) run();
+                cudaEventRecord(e1, ctx->stream);
+                MG_CK(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < best_ms) { best_ms = ms; best[2 * kern] = order; best[2 * kern + 1] = b; }
+            }
+        }
+        ctx->tune[p][kern][0] = best[2 * kern];
+        ctx->tune[p][kern][1] = best[2 * kern + 1];
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    mg_status st = check_launch(ctx);
+    if (st != MG_OK) return st;
+    g_tune_cache.push_back({key, best});
+    if (out) for (int k = 0; k < 4; k++) out[k] = best[k];
+    ctx->graph_dt = -1.0;  // the captured graph holds the old launch shapes
+    return MG_OK;
+}
+
+mg_status mg_set_tuning(mg_context *ctx, const int32_t tune[4]) {
+    if (!ctx || !tune) return MG_ERR_ARG;
+    for (int k = 0; k < 2; k++) {
+        const int order = tune[2 * k], b = tune[2 * k + 1];
+        if ((order != 0 && order != 1) || (b != 128 && b != 256 && b != 512)) return MG_ERR_ARG;
+        ctx->tune[ctx->precision][k][0] = order;
+        ctx->tune[ctx->precision][k][1] = b;
+    }
+    ctx->graph_dt = -1.0;
     return MG_OK;
 }
 

@@ -58,6 +58,8 @@ struct Geom {
     double thr;              // pow(0.2 a0, 2): displacement threshold of atom::decide
     double L[3];             // periodic lengths
     double inv_h;            // 2 / a0: inverse of the half lattice constant
+    float inv_h_f;           // 2 / a0 (float)
+    float thr_lo_f;          // thr * (1 - 1e-4) in float: FP32 distances below it skip the exact test
     float h_f;               // a0 / 2 (float)
     float rc2_h;             // (rc / h)^2 in half-lattice units
 };
@@ -95,10 +97,10 @@ struct Inter {
     int dcap;
     // per-slot claim word for recombination (INT_MAX when free)
     int *claim;
-    // lattice atoms farther than 0.2 a0 from their site (only recombined atoms after decide):
-    // they gather over the whole offset table and scatter the pairs the pruned gathers miss
+    // lattice atoms farther than 0.2 a0 from their site (only recombined atoms after decide): they
+    // and every atom within their full neighbourhood gather over the whole offset table
     int *far_list;
-    int8_t *far_flag;        // per slot, 1 for members of far_list
+    int8_t *far_flag;        // per slot: 1 for far atoms and their neighbourhoods
     int fcap;
     // buckets: sorted (key, ref) pairs; ref < cap: local index, else cap + ghost index
     long long *bucket;       // (key << 32) | ref packed, sorted ascending
@@ -168,6 +170,8 @@ OffsetTable make_offsets(int64_t size_x, int64_t size_y, int cut_lattice, double
 struct LaunchCtx {
     cudaStream_t stream;
     int num_sms;
+    int rho_order = 0, rho_block = 256;      // gather thread order and block size of the density pass
+    int force_order = 0, force_block = 256;  // the same for the force pass (chosen by mg_autotune)
 };
 
 // full: reference-order full tables (linear offsets); lat: the gather order (pruned entries first),
@@ -194,9 +198,8 @@ void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, Pot
                       bool mixed, bool hook);
 void launch_secondstep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams p, bool lattice);
 void launch_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed);
-// far atoms: rebuild the list from positions (uploads, hooks) and the scatter of missed pairs
+// far atoms: rebuild the list and its neighbourhood marks from positions (uploads, hooks)
 void launch_far_rebuild(const LaunchCtx &lc, const Geom &g, Slots s, Inter in);
-void launch_far_scatter(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, int kind, bool mixed);
 void launch_inter_manage(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, int steps_mask, bool mixed);
 enum { MANAGE_DECIDE = 1, MANAGE_CLEAR_GHOST = 2, MANAGE_EXCHANGE = 4, MANAGE_BORDER = 8, MANAGE_INDEX = 16 };
 void launch_inter_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed);

@@ -64,14 +64,28 @@ void set_constant_tables(const int *full_even, const int *full_odd, int n_full, 
 __device__ __forceinline__ int lin(const Geom &g, int x, int y, int z) { return (z * g.Sy + y) * g.Sx + x; }
 // parity-split index of a slot (x even and odd sites in two halves) for the mixed form's gather arrays
 __device__ __forceinline__ int sidx(const Geom &g, int s) { return (s & 1) * g.half + (s >> 1); }
-// Thread order of the gathers: all even local sites (k, j, i order), then all odd ones, so that a
-// warp has one parity and reads warp-uniform offsets.
-__device__ __forceinline__ int gather_slot(const Geom &g, int t, int &par) {
-    par = t >= g.n_local_half ? 1 : 0;
-    const int u = par ? t - g.n_local_half : t;
+// Thread order of the gathers. Warps always cover one site parity, so the candidate loop reads
+// warp-uniform offsets. Order 0: all even local sites (k, j, i order), then all odd ones. Order 1:
+// each run of 64 threads covers 32 consecutive even sites (first warp) and the 32 odd sites beside
+// them (second warp), so both halves of each output sector are written close in time. The
+// autotuner picks per kernel. Returns -1 past the end.
+__device__ __forceinline__ int gather_slot(const Geom &g, int t, int order, int &par) {
+    int u;
+    if (order) {
+        par = (t >> 5) & 1;
+        u = ((t >> 6) << 5) | (t & 31);  // index among the sites of this parity
+    } else {
+        par = t >= g.n_local_half ? 1 : 0;
+        u = par ? t - g.n_local_half : t;
+    }
+    if (u >= g.n_local_half) return -1;
     const int ih = u % g.nxh;
     const int r = u / g.nxh;
     return lin(g, 2 * ih + par + g.gx, r % g.by + g.gy, r / g.by + g.gz);
+}
+// threads to launch for the gathers
+inline int gather_threads(const Geom &g, int order) {
+    return order ? ((g.n_local_half + 31) / 32) * 64 : 2 * g.n_local_half;
 }
 
 __device__ __forceinline__ int local_slot(const Geom &g, int t, int &i, int &j, int &k) {
@@ -161,10 +175,8 @@ __device__ __forceinline__ double dt_inv_m_of(const StepParams &p, int type) {
 }
 __device__ __forceinline__ void set_error(Inter &in, uint32_t bit) { atomicOr((unsigned *) &in.cnt[CNT_ERRORS], bit); }
 // Lattice passes can fuse df / the half-kick only when no other kernel adds density or force to
-// lattice slots afterwards: no inter atoms and no far atoms.
-__device__ __forceinline__ bool lattice_only(const Inter &in) {
-    return in.cnt[CNT_INTER] == 0 && in.cnt[CNT_FAR] == 0;
-}
+// lattice slots afterwards, i.e. when there are no inter atoms.
+__device__ __forceinline__ bool lattice_only(const Inter &in) { return in.cnt[CNT_INTER] == 0; }
 // FP64 displacement test of atom::decide (src/atom.cpp:34-42) for a local slot
 __device__ __forceinline__ bool displaced_fp64(const Geom &g, const Slots &s, int sl) {
     const int X = sl % g.Sx, r = sl / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
@@ -203,6 +215,13 @@ __device__ __forceinline__ void locate_f(float x, float inv, int n, int &m, floa
     m = max(0, min(m, n - 2));
     p -= (float) m;
     p = fminf(p, 1.0f);
+}
+// knot of a pair distance in the FP32 gathers: 0 < r < rc <= (nr - 1) dr, so only a guard against
+// rounding at r ~ rc is needed (it keeps m on the last knot, whose record exists)
+__device__ __forceinline__ void locate_r_f(float x, float inv, int n, int &m, float &p) {
+    p = x * inv;
+    m = min((int) p, n - 1);
+    p -= (float) m;
 }
 __device__ __forceinline__ float val_f(const float4 *t, int m, float p) {
     const float4 c = __ldg(t + m);
@@ -314,11 +333,13 @@ __global__ void __launch_bounds__(256) k_firststep(Geom g, Slots s, Inter in, St
     double xs, ys, zs;
     site_of(g, i + g.gx, j + g.gy, k + g.gz, xs, ys, zs);
     const double ex = __dsub_rn(x, xs), ey = __dsub_rn(y, ys), ez = __dsub_rn(z, zs);
+    const float exf = __double2float_rn(ex), eyf = __double2float_rn(ey), ezf = __double2float_rn(ez);
     if (MIXED && MOVE) {
-        s.u4[sidx(g, sl)] = make_float4(__double2float_rn(__dmul_rn(ex, g.inv_h)), __double2float_rn(__dmul_rn(ey, g.inv_h)),
-                               __double2float_rn(__dmul_rn(ez, g.inv_h)), __int_as_float(ty));
+        const float ih = g.inv_h_f;
+        s.u4[sidx(g, sl)] = make_float4(exf * ih, eyf * ih, ezf * ih, __int_as_float(ty));
     }
-    if (DECIDE) {
+    // the exact FP64 test of decide runs only where the FP32 distance is not clearly below it
+    if (DECIDE && !(exf * exf + eyf * eyf + ezf * ezf < g.thr_lo_f)) {
         double dist = __dmul_rn(ex, ex);
         dist = __dadd_rn(dist, __dmul_rn(ey, ey));
         dist = __dadd_rn(dist, __dmul_rn(ez, ez));
@@ -465,11 +486,11 @@ __device__ __forceinline__ double rho_sum_fp64(const Geom &g, const Slots &s, co
     return acc;
 }
 
-__global__ void __launch_bounds__(256) k_lat_rho_fp64(Geom g, Slots s, Inter in, PotTables pt, bool hook) {
+__global__ void __launch_bounds__(512) k_lat_rho_fp64(Geom g, Slots s, Inter in, PotTables pt, bool hook, int order) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.n_local) return;
     int par;
-    const int sl = gather_slot(g, t, par);
+    const int sl = gather_slot(g, t, order, par);
+    if (sl < 0) return;
     const int ti = s.type[sl];
     if (ti < 0) { s.rho[sl] = 0.0; return; }
     const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
@@ -503,17 +524,17 @@ __device__ __forceinline__ void rho_sum_mixed(const Geom &g, const Slots &s, con
         if (r2 < rc2) {
             const float rp = r2 * rsqrtf(r2);
             int m; float p;
-            locate_f(rp, hinv, pt.nr, m, p);
+            locate_r_f(rp, hinv, pt.nr, m, p);
             kahan(sum, comp, val_f(pt.rho_vf + tj * pt.nr, m, p));
         }
     }
 }
 
-__global__ void __launch_bounds__(256) k_lat_rho_mixed(Geom g, Slots s, Inter in, PotTables pt, bool hook) {
+__global__ void __launch_bounds__(512) k_lat_rho_mixed(Geom g, Slots s, Inter in, PotTables pt, bool hook, int order) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.n_local) return;
     int par;
-    const int sl = gather_slot(g, t, par);
+    const int sl = gather_slot(g, t, order, par);
+    if (sl < 0) return;
     const int si = sidx(g, sl);
     const float4 ui = s.u4[si];
     const int ti = __float_as_int(ui.w);
@@ -537,9 +558,9 @@ __global__ void __launch_bounds__(256) k_lat_rho_mixed(Geom g, Slots s, Inter in
 }
 
 void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook) {
-    const int b = 256, n = (g.n_local + b - 1) / b;
-    if (mixed) k_lat_rho_mixed<<<n, b, 0, lc.stream>>>(g, s, in, t, hook);
-    else k_lat_rho_fp64<<<n, b, 0, lc.stream>>>(g, s, in, t, hook);
+    const int order = lc.rho_order, b = lc.rho_block, n = (gather_threads(g, order) + b - 1) / b;
+    if (mixed) k_lat_rho_mixed<<<n, b, 0, lc.stream>>>(g, s, in, t, hook, order);
+    else k_lat_rho_fp64<<<n, b, 0, lc.stream>>>(g, s, in, t, hook, order);
 }
 
 // dF/drho when inter atoms added density after the lattice pass (or for the df hook)
@@ -608,12 +629,12 @@ __device__ __forceinline__ void force_sum_fp64(const Geom &g, const Slots &s, co
     }
 }
 
-__global__ void __launch_bounds__(256) k_lat_force_fp64(Geom g, Slots s, Inter in, PotTables pt, StepParams sp,
-                                                        bool kick, bool hook) {
+__global__ void __launch_bounds__(512) k_lat_force_fp64(Geom g, Slots s, Inter in, PotTables pt, StepParams sp,
+                                                        bool kick, bool hook, int order) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.n_local) return;
     int par;
-    const int sl = gather_slot(g, t, par);
+    const int sl = gather_slot(g, t, order, par);
+    if (sl < 0) return;
     const int ti = s.type[sl];
     if (ti < 0) { s.fx[sl] = 0.0; s.fy[sl] = 0.0; s.fz[sl] = 0.0; return; }
     const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
@@ -656,7 +677,7 @@ __device__ __forceinline__ void force_sum_mixed(const Geom &g, const Slots &s, c
             const float rinv_h = rsqrtf(r2);
             const float rp = r2 * rinv_h;
             int m; float p;
-            locate_f(rp, hinv, pt.nr, m, p);
+            locate_r_f(rp, hinv, pt.nr, m, p);
             const float rhojp = der_f(pt.rho_dff + tj * pt.nr, m, p);
             const float rhoip = (tj == ti) ? rhojp : der_f(rho_di, m, p);
             const int pr = (ti * 3 + tj) * pt.nr;
@@ -674,12 +695,12 @@ __device__ __forceinline__ void force_sum_mixed(const Geom &g, const Slots &s, c
     }
 }
 
-__global__ void __launch_bounds__(256) k_lat_force_mixed(Geom g, Slots s, Inter in, PotTables pt, StepParams sp,
-                                                         bool kick, bool hook) {
+__global__ void __launch_bounds__(512) k_lat_force_mixed(Geom g, Slots s, Inter in, PotTables pt, StepParams sp,
+                                                         bool kick, bool hook, int order) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.n_local) return;
     int par;
-    const int sl = gather_slot(g, t, par);
+    const int sl = gather_slot(g, t, order, par);
+    if (sl < 0) return;
     const int si = sidx(g, sl);
     const float4 ui = s.u4[si];
     const int ti = __float_as_int(ui.w);
@@ -709,9 +730,9 @@ __global__ void __launch_bounds__(256) k_lat_force_mixed(Geom g, Slots s, Inter 
 
 void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams p, bool kick,
                       bool mixed, bool hook) {
-    const int b = 256, n = (g.n_local + b - 1) / b;
-    if (mixed) k_lat_force_mixed<<<n, b, 0, lc.stream>>>(g, s, in, t, p, kick, hook);
-    else k_lat_force_fp64<<<n, b, 0, lc.stream>>>(g, s, in, t, p, kick, hook);
+    const int order = lc.force_order, b = lc.force_block, n = (gather_threads(g, order) + b - 1) / b;
+    if (mixed) k_lat_force_mixed<<<n, b, 0, lc.stream>>>(g, s, in, t, p, kick, hook, order);
+    else k_lat_force_fp64<<<n, b, 0, lc.stream>>>(g, s, in, t, p, kick, hook, order);
 }
 
 // second half-kick for lattice slots (only when inter atoms prevented fusion, or always) and for
@@ -788,11 +809,11 @@ __device__ __forceinline__ void energy_sum_mixed(const Geom &g, const Slots &s, 
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(256) k_energy(Geom g, Slots s, Inter in, PotTables pt) {
+__global__ void __launch_bounds__(256) k_energy(Geom g, Slots s, Inter in, PotTables pt, int order) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.n_local) return;
     int par;
-    const int sl = gather_slot(g, t, par);
+    const int sl = gather_slot(g, t, order, par);
+    if (sl < 0) return;
     const int ti = s.type[sl];
     if (ti < 0) { s.e[sl] = 0.0; return; }
     const int np = c_npruned;
@@ -819,9 +840,29 @@ __global__ void __launch_bounds__(256) k_energy(Geom g, Slots s, Inter in, PotTa
     }
 }
 void launch_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
-    const int b = 256, n = (g.n_local + b - 1) / b;
-    if (mixed) k_energy<true><<<n, b, 0, lc.stream>>>(g, s, in, t);
-    else k_energy<false><<<n, b, 0, lc.stream>>>(g, s, in, t);
+    const int b = 256, n = (gather_threads(g, 0) + b - 1) / b;
+    if (mixed) k_energy<true><<<n, b, 0, lc.stream>>>(g, s, in, t, 0);
+    else k_energy<false><<<n, b, 0, lc.stream>>>(g, s, in, t, 0);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Far atoms: lattice atoms farther than 0.2 a0 from their site (after decide, only recombined
+// atoms). Pairs beyond the pruned table can reach them, so the atom itself and the owner of every
+// slot of its full neighbourhood get far_flag = 1: their gathers also run the tail of the table.
+// (A normal atom k sees a far atom i across the periodic boundary through i's ghost image; k is the
+// owner of a ghost slot in i's neighbourhood, so it is marked too.) Clearing writes 0 over the same
+// slots of the old list. Work item e of a flat loop covers (far atom e / (nfull + 1), entry).
+// ------------------------------------------------------------------------------------------------
+__device__ void mark_far_neighbourhoods(const Geom &g, const Inter &in, int a0, int a1, int8_t v, int t0, int nt) {
+    const int per = c_nfull + 1;
+    const int total = (a1 - a0) * per;
+    for (int e = t0; e < total; e += nt) {
+        const int sl = in.far_list[a0 + e / per];
+        const int q = e % per;
+        const int par = (sl % g.Sx) & 1;
+        const int sj = q == c_nfull ? sl : sl + (par ? c_lat[1][q] : c_lat[0][q]);
+        in.far_flag[owner_slot(g, sj)] = v;
+    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -920,7 +961,7 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s
         // the far list of the previous step is void: every lattice atom is re-tested below
         {
             const int nf = min(in.cnt[CNT_FAR], in.fcap);
-            for (int q = tid; q < nf; q += nt) in.far_flag[in.far_list[q]] = 0;
+            mark_far_neighbourhoods(g, in, 0, nf, 0, tid, nt);
             __syncthreads();
             if (tid == 0) in.cnt[CNT_FAR] = 0;
             __syncthreads();
@@ -989,10 +1030,12 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s
             // a recombined atom may sit up to sqrt(5)/4 a0 from its new site
             if (displaced_fp64(g, s, sl)) {
                 const int q = atomicAdd(&in.cnt[CNT_FAR], 1);
-                if (q < in.fcap) { in.far_list[q] = sl; in.far_flag[sl] = 1; }
+                if (q < in.fcap) in.far_list[q] = sl;
                 else set_error(in, MG_DEVERR_DISPLACED_OVERFLOW);
             }
         }
+        __syncthreads();
+        mark_far_neighbourhoods(g, in, 0, min(in.cnt[CNT_FAR], in.fcap), 1, tid, nt);
         __syncthreads();
         // stable compaction of the survivors
         int base = 0;
@@ -1271,9 +1314,9 @@ void launch_inter_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, 
 // far lattice atoms (farther than 0.2 a0 from their site). Rebuild from positions for states that did
 // not come through atom::decide (uploads, the per-phase hooks).
 // ------------------------------------------------------------------------------------------------
-__global__ void k_far_clear(Inter in) {
+__global__ void k_far_clear(Geom g, Inter in) {
     const int nf = min(in.cnt[CNT_FAR], in.fcap);
-    for (int q = threadIdx.x; q < nf; q += blockDim.x) in.far_flag[in.far_list[q]] = 0;
+    mark_far_neighbourhoods(g, in, 0, nf, 0, threadIdx.x, blockDim.x);
     __syncthreads();
     if (threadIdx.x == 0) in.cnt[CNT_FAR] = 0;
 }
@@ -1285,66 +1328,21 @@ __global__ void k_far_scan(Geom g, Slots s, Inter in) {
     if (s.type[sl] < 0) return;
     if (displaced_fp64(g, s, sl)) {
         const int q = atomicAdd(&in.cnt[CNT_FAR], 1);
-        if (q < in.fcap) { in.far_list[q] = sl; in.far_flag[sl] = 1; }
+        if (q < in.fcap) in.far_list[q] = sl;
         else set_error(in, MG_DEVERR_DISPLACED_OVERFLOW);
     }
 }
+__global__ void k_far_mark(Geom g, Inter in) {
+    const int nf = min(in.cnt[CNT_FAR], in.fcap);
+    mark_far_neighbourhoods(g, in, 0, nf, 1, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
 void launch_far_rebuild(const LaunchCtx &lc, const Geom &g, Slots s, Inter in) {
-    k_far_clear<<<1, 1024, 0, lc.stream>>>(in);
+    k_far_clear<<<1, 1024, 0, lc.stream>>>(g, in);
     const int b = 256;
     k_far_scan<<<(g.n_local + b - 1) / b, b, 0, lc.stream>>>(g, s, in);
+    k_far_mark<<<lc.num_sms, 256, 0, lc.stream>>>(g, in);
 }
 
-// Pairs between a far atom i and a lattice atom j whose sites are beyond the pruned radius: j's
-// pruned gather does not see them, so i adds j's share (FP64, to j's owner). Skipped when j's owner
-// is itself far (its full gather sees i). kind: 0 density, 1 force, 2 energy.
-template <int KIND>
-__global__ void k_far_scatter(Geom g, Slots s, Inter in, PotTables pt, bool mixed) {
-    const int nf = min(in.cnt[CNT_FAR], in.fcap);
-    const int nfull = c_nfull, np = c_npruned;
-    for (int q0 = blockIdx.x * blockDim.x + threadIdx.x; q0 < nf; q0 += gridDim.x * blockDim.x) {
-        const int sl = in.far_list[q0];
-        const int ti = s.type[sl];
-        if (ti < 0) continue;
-        const int par = (sl % g.Sx) & 1;
-        const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
-        const double dfi = lat_df(g, s, sl, mixed);
-        for (int q = np; q < nfull; q++) {
-            const int sj = sl + (par ? c_lat[1][q] : c_lat[0][q]);
-            const int tj = s.type[sj];
-            if (tj < 0) continue;
-            const int own = owner_slot(g, sj);
-            if (in.far_flag[own]) continue;
-            const double dx = xi - s.x[sj], dy = yi - s.y[sj], dz = zi - s.z[sj];
-            const double r2 = dx * dx + dy * dy + dz * dz;
-            if (!(r2 < g.rc2)) continue;
-            const double r = sqrt(r2);
-            int m; double p;
-            locate_d(r, pt.inv_dr, pt.nr, m, p);
-            if (KIND == 0) {
-                atomicAdd(&s.rho[own], val_d(pt.rho_v + ti * pt.nr, m, p));
-            } else if (KIND == 1) {
-                const double dfj = lat_df(g, s, sj, mixed);
-                const double rhoip = der_d(pt.rho_d + ti * pt.nr, m, p), rhojp = der_d(pt.rho_d + tj * pt.nr, m, p);
-                const double zv = val_d(pt.z_v + (ti * 3 + tj) * pt.nr, m, p), zp = der_d(pt.z_d + (ti * 3 + tj) * pt.nr, m, p);
-                const double recip = 1.0 / r;
-                const double phi = zv * recip;
-                const double phip = zp * recip - phi * recip;
-                const double fp = -(dfi * rhojp + dfj * rhoip + phip) * recip;
-                atomicAdd(&s.fx[own], -dx * fp);
-                atomicAdd(&s.fy[own], -dy * fp);
-                atomicAdd(&s.fz[own], -dz * fp);
-            } else {
-                atomicAdd(&s.e[own], 0.5 * val_d(pt.z_v + (ti * 3 + tj) * pt.nr, m, p) / r);
-            }
-        }
-    }
-}
-void launch_far_scatter(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, int kind, bool mixed) {
-    if (kind == 0) k_far_scatter<0><<<lc.num_sms, 128, 0, lc.stream>>>(g, s, in, t, mixed);
-    else if (kind == 1) k_far_scatter<1><<<lc.num_sms, 128, 0, lc.stream>>>(g, s, in, t, mixed);
-    else k_far_scatter<2><<<lc.num_sms, 128, 0, lc.stream>>>(g, s, in, t, mixed);
-}
 
 // ------------------------------------------------------------------------------------------------
 // setv (src/atom.cpp:475-494): one thread

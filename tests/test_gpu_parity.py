@@ -388,3 +388,26 @@ def test_bad_inputs_are_rejected(pkg, wl, potentials, gpu_lib, tmp_path):
     with pytest.raises(pkg.MgError):
         pkg.Context((4, 6, 6), A0, RCF)  # narrower than 2 ghost widths
     ctx.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_autotune_keeps_results_bit_identical(pkg, wl, potentials, gpu_lib, prec):
+    cells = (14, 12, 13)
+    atoms = wl.build_state(cells, A0, RCF, temperature=600.0, seed=81, cu_frac=0.02, ni_frac=0.01)
+    runs = []
+    for tune in (None, (1, 128, 1, 512), "auto"):
+        ctx = pkg.Context(cells, A0, RCF, precision=prec)
+        ctx.pot_init_setfl(potentials["fecuni"])
+        ctx.upload(atoms)
+        ctx.prepare()
+        if tune == "auto":
+            t = ctx.autotune(reps=2)
+            assert t["rho_order"] in (0, 1) and t["force_block"] in (128, 256, 512)
+        elif tune is not None:
+            ctx.set_tuning(*tune)
+        ctx.simulate(5)
+        got, _ = ctx.download()
+        runs.append(got)
+        ctx.close()
+    for r in runs[1:]:
+        assert np.array_equal(r["x"], runs[0]["x"]) and np.array_equal(r["f"], runs[0]["f"])
