@@ -56,6 +56,15 @@ def parse():
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     p.add_argument("--resident-only", action="store_true",
                    help="time only the resident step (no accuracy, FP64, drift, e2e or CPU legs)")
+    p.add_argument("--no-drift", action="store_true")
+    p.add_argument("--drift-equil", type=int, default=200)
+    p.add_argument("--drift-steps", type=int, default=1000)
+    p.add_argument("--drift-every", type=int, default=100)
+    p.add_argument("--no-cascades", action="store_true")
+    p.add_argument("--cascade-window", type=int, default=150)
+    p.add_argument("--cascade-graph-steps", type=int, default=10)
+    p.add_argument("--cascade-fp64-steps", type=int, default=200)
+    p.add_argument("--cascade-fp64-replicas", type=int, default=8)
     return p.parse_args()
 
 
@@ -208,6 +217,180 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def _events(torch):
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def time_on_stream(torch, device, stream_handle, fn):
+    """CUDA-event time (ms) of the work fn() enqueues on the given library stream."""
+    stream = torch.cuda.ExternalStream(stream_handle, device=device)
+    e0, e1 = _events(torch)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def drift_leg(pkg, w, pot, precision, equil, steps, every, seed):
+    """NVE total energy per atom against time after `equil` steps; slope by least squares."""
+    wl = pkg.workloads
+    atoms = wl.workload_state(w, seed=seed)
+    c = pkg.Context(w.cells, w.lattice_const, w.cutoff_radius_factor, precision=precision)
+    c.pot_init_setfl(pot)
+    c.set_timestep(w.dt)
+    c.upload(atoms)
+    del atoms
+    c.prepare()
+    c.autotune(reps=1)
+    c.simulate(equil, sync=True)
+    t, e = [], []
+    for k in range(steps // every + 1):
+        th = c.thermo(with_energy=True)
+        t.append(k * every * w.dt)
+        e.append((th["potential_energy"] + th["kinetic_energy"] * wl.MVV2E) / w.n_atoms)
+        if k < steps // every:
+            c.simulate(every, sync=True)
+    c.close()
+    t, e = np.array(t), np.array(e)
+    slope, icpt = np.polyfit(t, e, 1)
+    return {"workload": w.name, "atoms": w.n_atoms, "precision": precision,
+            "ev_per_atom_per_ps": float(slope), "span_ps": float(t[-1]), "points": len(t),
+            "equilibration_steps": equil, "fluctuation_rms_ev_per_atom": float(np.std(e - (slope * t + icpt))),
+            "e_total_ev_per_atom": float(e[0])}
+
+
+def cascade_ctx(pkg, cells, a0, rcf, pot, atoms, precision, lat, direction, energy, cap=32768, tune_reps=1):
+    wl = pkg.workloads
+    c = pkg.Context(cells, a0, rcf, precision=precision, inter_capacity=cap)
+    c.pot_init_setfl(pot)
+    c.upload(atoms)
+    c.prepare()
+    if tune_reps:
+        c.autotune(reps=tune_reps)
+    c.collision_step(lat, direction, energy)
+    c.set_variable_timestep(wl.CASCADE_DX_MAX, wl.CASCADE_DT_MIN, wl.CASCADE_DT_MAX)
+    return c
+
+
+def cascade_leg(args, pkg, torch, device, tmp):
+    """Single 5 keV cascade (2M atoms) and the 64-replica cascade set: batched mixed against
+    sequential single-cascade runs."""
+    wl = pkg.workloads
+    out = {}
+    # ---- one cascade, 100^3 Fe, 5 keV ----
+    w3 = wl.WORKLOADS["fe_100c_cascade"]
+    pot3 = wl.workload_potential(w3, tmp)
+    st3 = wl.workload_state(w3)
+    lat3 = [w3.cells[0] // 2, w3.cells[1] // 2, w3.cells[2] // 2, 0]
+    dir3 = wl.pka_direction(w3.seed)
+    c = cascade_ctx(pkg, w3.cells, w3.lattice_const, w3.cutoff_radius_factor, pot3, st3, "mixed", lat3, dir3,
+                    w3.pka_ev, tune_reps=2)
+    c.simulate(1, sync=True)
+    ms = time_on_stream(torch, device, c.stream(), lambda: c.simulate(w3.steps - 1, sync=False))
+    c.simulate(0, sync=True)  # raises if a capacity was exceeded
+    steps3, t3, _ = c.clock()
+    th = c.thermo()
+    hist = c.dt_history(w3.steps)
+    c.close()
+    c = cascade_ctx(pkg, w3.cells, w3.lattice_const, w3.cutoff_radius_factor, pot3, st3, "fp64", lat3, dir3,
+                    w3.pka_ev, tune_reps=1)
+    c.simulate(1, sync=True)
+    n64 = args.cascade_fp64_steps
+    ms64 = time_on_stream(torch, device, c.stream(), lambda: c.simulate(n64, sync=False))
+    c.close()
+    del st3
+    ms64_full = ms64 / n64 * (w3.steps - 1)
+    out["single"] = {
+        "workload": f"{w3.name}: BCC Fe {w3.cells[0]}^3 cells = {w3.n_atoms} atoms, {w3.temperature:.0f} K, "
+                    f"PKA {w3.pka_ev:.0f} eV at the central site, dt = clamp(0.01 A / max|v|, 0.01 fs, 1 fs), "
+                    f"{w3.steps} steps",
+        "mixed_s": ms / 1e3, "mixed_steps_timed": w3.steps - 1, "simulated_ps": t3, "steps": steps3,
+        "dt_fs_first_last": [hist[0] * 1e3, hist[-1] * 1e3], "inter_atoms_at_end": th["n_inter"],
+        "fp64_s_est": ms64_full / 1e3, "fp64_sample_steps": n64,
+        "mixed_over_fp64": ms64_full / ms,
+        "atom_steps_per_s_mixed": w3.n_atoms * (w3.steps - 1) / (ms / 1e3)}
+
+    # ---- 64 replicas: batched mixed vs sequential ----
+    cs = wl.CASCADE_SETS["fecuni_cascades_64"]
+    specs = cs.replica_specs()
+    pot4 = wl.workload_potential(cs.potential_workload(), tmp)
+    a0, rcf = cs.lattice_const, cs.cutoff_radius_factor
+    states = [wl.build_state(sp["cells"], a0, rcf, temperature=cs.temperature, seed=sp["seed"],
+                             cu_frac=cs.cu_frac, ni_frac=cs.ni_frac) for sp in specs]
+    atoms_r = np.array([2 * sp["cells"][0] ** 3 for sp in specs], dtype=np.float64)
+    ctxs = [cascade_ctx(pkg, sp["cells"], a0, rcf, pot4, st, "mixed", sp["lat"], sp["dir"], sp["energy"])
+            for sp, st in zip(specs, states)]
+
+    def reset():
+        for c, sp, st in zip(ctxs, specs, states):
+            c.upload(st)
+            c.prepare()
+            c.collision_step(sp["lat"], sp["dir"], sp["energy"])
+            c.set_variable_timestep(wl.CASCADE_DX_MAX, wl.CASCADE_DT_MIN, wl.CASCADE_DT_MAX)
+
+    batch = pkg.Batch(ctxs, steps_per_launch=args.cascade_graph_steps)
+    batch.run(3)
+    ms_b = time_on_stream(torch, device, batch.stream(), lambda: batch.run(cs.steps, sync=False))
+    batch.run(0)  # raises with the replica index if one overflowed
+    clocks = [c.clock() for c in ctxs]
+    inter = [c.thermo()["n_inter"] for c in ctxs]
+    # the same window of steps, batched and one replica after another (mixed)
+    win = args.cascade_window
+    reset()
+    batch.run(3)
+    ms_bw = time_on_stream(torch, device, batch.stream(), lambda: batch.run(win, sync=False))
+    reset()
+    for c in ctxs:
+        c.simulate(3, sync=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for c in ctxs:
+        c.simulate(win, sync=True)
+    s_sw = time.perf_counter() - t0
+    batch.close()
+    for c in ctxs:
+        c.close()
+    del ctxs
+    # sequential plain FP64: a size-stratified sample of replicas, one after another
+    order = np.argsort(atoms_r)
+    pick = [int(order[k]) for k in np.linspace(0, len(specs) - 1, args.cascade_fp64_replicas).round().astype(int)]
+    s64, atoms64 = 0.0, 0.0
+    for r in pick:
+        sp = specs[r]
+        c = cascade_ctx(pkg, sp["cells"], a0, rcf, pot4, states[r], "fp64", sp["lat"], sp["dir"], sp["energy"])
+        c.simulate(3, sync=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c.simulate(win, sync=True)
+        s64 += time.perf_counter() - t0
+        atoms64 += atoms_r[r]
+        c.close()
+    del states
+    seq64_full_s = s64 / atoms64 * atoms_r.sum() * (cs.steps / win)
+    batched_s = ms_b / 1e3
+    out["batched"] = {
+        "set": f"{cs.name}: {cs.replicas} Fe-1.5Cu-1.0Ni replicas, cubic edges U{{{cs.cells_lo}..{cs.cells_hi}}} cells "
+               f"({int(atoms_r.sum())} atoms in all), {cs.temperature:.0f} K, PKA U[{cs.energy_lo:.0f}, {cs.energy_hi:.0f}] eV, "
+               f"per-replica variable dt, {cs.steps} steps each",
+        "batched_mixed_s": batched_s,
+        "cascades_per_hour_batched_mixed": cs.replicas * 3600.0 / batched_s,
+        "sequential_fp64_s_est": seq64_full_s,
+        "cascades_per_hour_sequential_fp64": cs.replicas * 3600.0 / seq64_full_s,
+        "batched_mixed_over_sequential_fp64": seq64_full_s / batched_s,
+        "sequential_fp64_sample": f"{len(pick)} replicas (size-stratified) x {win} steps, scaled by atoms and steps",
+        "window": {"steps": win, "batched_mixed_s": ms_bw / 1e3, "sequential_mixed_s": s_sw,
+                   "batching_gain": s_sw / (ms_bw / 1e3)},
+        "graph_steps_per_launch": args.cascade_graph_steps,
+        "atom_steps_per_s_batched": float(atoms_r.sum()) * cs.steps / batched_s,
+        "simulated_ps_min_median_max": [min(k[1] for k in clocks), float(np.median([k[1] for k in clocks])),
+                                        max(k[1] for k in clocks)],
+        "inter_atoms_at_end_max": int(max(inter)),
+    }
+    return out
+
+
 def run_ours(args):
     rank, world, dist = dist_init(args.gpus)
     import torch
@@ -248,32 +431,26 @@ def run_ours(args):
         tuning[prec] = c.autotune(reps=2)  # cached per (box, precision) after the first call
         return c
 
-    # ---- resident ----
+    # ---- resident: CUDA-graph replay of the loop body, inputs in HBM ----
     ctx = make_ctx(args.precision)
     ctx.simulate(args.warmup, sync=True)
-    stream = torch.cuda.ExternalStream(ctx.stream(), device=device)
-    ctx.enable_timing(True)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     sampler = ClockSampler(local_rank)
     sampler.start()
     time.sleep(0.4)
     barrier(dist, device)
-    torch.cuda.synchronize()
-    ev0.record(stream)
-    ctx.simulate(args.steps, sync=False)
-    ev1.record(stream)
-    ev1.synchronize()
-    torch.cuda.synchronize()
+    ms_total = time_on_stream(torch, device, ctx.stream(), lambda: ctx.simulate(args.steps, sync=False))
     barrier(dist, device)
     clocks = sampler.stop()
-    ms_total = ev0.elapsed_time(ev1)
     ms_total = reduce_max(dist, ms_total, device)
     ms_per_step = ms_total / args.steps
+    launches = ctx.launches_per_step() * args.steps
+    value = world * n_atoms * args.steps / (ms_total / 1e3)
+    # ---- the same steps with CUDA events around every kernel (per-kernel times, roofline) ----
+    ctx.enable_timing(True)
+    ms_instr = time_on_stream(torch, device, ctx.stream(), lambda: ctx.simulate(args.steps, sync=False))
     kt = ctx.kernel_times()
     ctx.enable_timing(False)
     thermo = ctx.thermo()
-    launches = ctx.launches_per_step() * args.steps
-    value = world * n_atoms * args.steps / (ms_total / 1e3)
 
     force_ms = kt.get("lat_force", float("nan"))
     achieved = BYTES_PER_ATOM_FORCE_SWEEP * n_atoms / (force_ms / 1e3) / 1e9
@@ -282,7 +459,8 @@ def run_ours(args):
         ctx.close()
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                              "ms_per_step": ms_per_step, "precision": args.precision, "workload": w.name,
+                              "ms_per_step": ms_per_step, "ms_per_step_instrumented": ms_instr / args.steps,
+                              "precision": args.precision, "workload": w.name,
                               "kernel_ms_per_step": kt, "roofline_achieved_gbs": achieved, "clocks": clocks,
                               "tuning": tuning}))
         return
@@ -301,33 +479,10 @@ def run_ours(args):
 
     # ---- plain FP64, resident ----
     ctx64.simulate(2, sync=True)
-    s64 = torch.cuda.ExternalStream(ctx64.stream(), device=device)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(s64)
-    ctx64.simulate(args.fp64_steps, sync=False)
-    e1.record(s64)
-    e1.synchronize()
-    ms64 = reduce_max(dist, e0.elapsed_time(e1), device) / args.fp64_steps
+    ms64 = time_on_stream(torch, device, ctx64.stream(), lambda: ctx64.simulate(args.fp64_steps, sync=False))
+    ms64 = reduce_max(dist, ms64, device) / args.fp64_steps
     value64 = world * n_atoms / (ms64 / 1e3)
     ctx64.close()
-
-    # ---- energy drift of the mixed form (outside the timed region) ----
-    drift = None
-    try:
-        ctxd = make_ctx("mixed")
-        series = []
-        for k in range(6):
-            th = ctxd.thermo(with_energy=True)
-            series.append((k * 20 * w.dt, (th["potential_energy"] + th["kinetic_energy"] * wl.MVV2E) / n_atoms))
-            ctxd.simulate(20, sync=True)
-        t = np.array([s[0] for s in series])
-        e = np.array([s[1] for s in series])
-        slope = float(np.polyfit(t, e, 1)[0])
-        drift = {"ev_per_atom_per_ps": slope, "span_ps": float(t[-1]), "points": len(t)}
-        ctxd.close()
-    except Exception as exc:  # keep the bench line even if the drift pass fails
-        drift = {"error": str(exc)}
 
     # ---- end to end through the drop-in call (host slot array, pinned) ----
     host = atoms.copy()
@@ -345,14 +500,44 @@ def run_ours(args):
     e2e_ctx.close()
     e2e_value = world * n_atoms * args.e2e_steps / e2e_s
     bytes_io = host.nbytes + n_inter * pkg.ATOM_DTYPE.itemsize
+    del host
+    ctx.close()
+    del atoms
+
+    # ---- NVE energy drift (outside the timed regions) ----
+    drift = {}
+    if not args.no_drift:
+        import dataclasses
+        small = dataclasses.replace(w, cells=(100, 100, 100), name=f"{w.name}@100c")
+        pot_small = wl.workload_potential(small, tmp)
+        for key, ww, pp, prec in (("mixed", w, pot, "mixed"), ("mixed_2M", small, pot_small, "mixed"),
+                                  ("fp64_2M", small, pot_small, "fp64")):
+            try:
+                drift[key] = drift_leg(pkg, ww, pp, prec, args.drift_equil, args.drift_steps, args.drift_every,
+                                       seed=w.seed + rank)
+            except Exception as exc:  # keep the bench line if a drift pass fails
+                drift[key] = {"error": str(exc)}
+
+    # ---- cascades: one 2M-atom cascade and the 64-replica set (rank 0 of a one-GPU run) ----
+    cascades = None
+    if world == 1 and not args.no_cascades:
+        try:
+            cascades = cascade_leg(args, pkg, torch, device, tmp)
+        except Exception as exc:
+            cascades = {"error": f"{type(exc).__name__}: {exc}"}
 
     cb = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(w, pot, args.cpu_seconds)
 
-    ctx.close()
     if rank != 0:
         return
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "lat_force_mixed_traffic.json")))
+        traffic = tr["dram_bytes_per_launch"] / tr["atoms"] * n_atoms
+    except (OSError, ValueError, KeyError):
+        pass
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -361,19 +546,24 @@ def run_ours(args):
                                f"{w.temperature:.0f} K Maxwell start, dt {w.dt * 1000:.0f} fs, synthetic 3-element setfl "
                                f"(nr = nrho = 5000, rc 5.6 A)",
                    "precision": "mixed", "l2": "working set ~1.9 GB > 129 MB L2 (no flush needed)",
+                   "timing": "value: CUDA-graph replay timed with CUDA events on the library stream; kernel times: "
+                             "a second pass of the same steps with events around every kernel",
                    "parallelism": f"{world} independent replica(s), one per GPU"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io,
                 "path": "mg_step_host: pinned host slot array in, one loop body, slot array out"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None,
+                     "frac": achieved / hbm_peak, "traffic": traffic,
                      "kernel": "lat_force (mixed)", "kernel_ms": force_ms,
                      "bytes_per_atom": BYTES_PER_ATOM_FORCE_SWEEP, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                     "traffic_source": "profiles/lat_force_mixed_traffic.json (ncu dram bytes, scaled by atoms)",
                      "step_achieved_gbs": step_achieved, "step_frac": step_achieved / hbm_peak},
         "kernel_ms_per_step": kt,
+        "ms_per_step_instrumented": ms_instr / args.steps,
         "fp64": {"value": value64, "ms_per_step": ms64, "steps": args.fp64_steps},
         "mixed_over_fp64": value / value64,
         "accuracy": {"force_rms_ev_per_A": f_rms, "force_max_ev_per_A": f_max, "reference": "FP64 GPU form",
                      "nve_drift": drift},
+        "cascades": cascades,
         "gpu_launches": launches,
         "tuning": tuning,
         "clocks": clocks,

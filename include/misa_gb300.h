@@ -133,8 +133,17 @@ mg_status mg_download(mg_context *ctx, mg_atom_element *atoms, int64_t n_slots, 
                       int64_t inter_cap, int64_t *n_inter);
 /* Ghost inter atoms (type, x, df; other fields 0), list order. */
 mg_status mg_download_ghost_inter(mg_context *ctx, mg_atom_element *ghost, int64_t cap, int64_t *n_ghost);
-/* NewtonMotion::setTimestepLength (src/newton_motion.cpp:13-17), dt in ps. */
+/* NewtonMotion::setTimestepLength (src/newton_motion.cpp:13-17), dt in ps. Fixed dt from the next step. */
 mg_status mg_set_timestep(mg_context *ctx, double dt_ps);
+/* Variable timestep (extension; the reference changes dt only per stage, frontend/md_simulation.cpp:42-58).
+ * Before each step, dt = clamp(dx_max / max|v|, dt_min, dt_max), max over local lattice and inter atoms,
+ * computed on the device as (vx^2 + vy^2) + vz^2, sqrt, divide, each correctly rounded. Units: Angstrom,
+ * ps. mg_set_timestep returns to a fixed dt. */
+mg_status mg_set_variable_timestep(mg_context *ctx, double dx_max, double dt_min_ps, double dt_max_ps);
+/* Steps taken since creation, simulated time (sum of the dt used) and the dt of the last step. Syncs. */
+mg_status mg_clock(mg_context *ctx, int64_t *steps, double *time_ps, double *dt_ps);
+/* The dt of the most recent min(steps, cap, 65536) steps, oldest first; *n_out = how many. Syncs. */
+mg_status mg_dt_history(mg_context *ctx, double *out, int64_t cap, int64_t *n_out);
 /* simulation::prepareForStart body (src/simulation.cpp:209-219): first ghost exchange, computeEam. */
 mg_status mg_prepare(mg_context *ctx);
 /* nsteps iterations of the loop body (src/simulation.cpp:241-265): firststep, decide, exchangeInter,
@@ -203,6 +212,26 @@ mg_status mg_kernel_times(const mg_context *ctx, double *ms, int32_t cap, int32_
 mg_status mg_launches_per_step(const mg_context *ctx, int32_t *n);
 /* CUDA stream of the context (a cudaStream_t), for callers timing on it. */
 void *mg_stream(const mg_context *ctx);
+
+/* ---- Batched independent replicas (extension, no reference counterpart: the reference runs one
+ * simulation per MPI job). One CUDA graph holds the loop body (mg_simulate's step) of every context
+ * as its own branch, steps_per_launch bodies deep, so one graph launch advances all replicas; their
+ * small kernels (inter-atom list, PKA region) overlap instead of running back to back. Boxes,
+ * precisions and timestep rules may differ per replica; every context must be prepared, and must
+ * outlive the batch. Work a caller issues on a member context is ordered before or after
+ * mg_batch_run as the calls are made. A member whose precision, tuning or potential changed is
+ * recaptured at the next run. ---- */
+typedef struct mg_batch mg_batch;
+mg_status mg_batch_create(mg_context *const *ctxs, int32_t n, int32_t steps_per_launch, mg_batch **out);
+/* nsteps loop bodies of every replica; sync != 0 waits and reports the first replica whose device
+ * error word is set (message via mg_batch_last_error). */
+mg_status mg_batch_run(mg_batch *b, int64_t nsteps, int32_t sync);
+/* graph nodes per step of all replicas together */
+mg_status mg_batch_launches_per_step(const mg_batch *b, int32_t *n);
+void *mg_batch_stream(const mg_batch *b);
+const char *mg_batch_last_error(const mg_batch *b);
+mg_status mg_batch_destroy(mg_batch *b);
+
 /* Page-lock a host range (the caller's slot array) so mg_step_host / mg_upload / mg_download copy it
  * by DMA; undo with mg_host_unregister before freeing it. */
 mg_status mg_host_register(void *ptr, uint64_t bytes);

@@ -75,6 +75,9 @@ _PROTOS = {
     "mg_download": (_I32, [_P, _P, _I64, _P, _I64, _P]),
     "mg_download_ghost_inter": (_I32, [_P, _P, _I64, _P]),
     "mg_set_timestep": (_I32, [_P, _D]),
+    "mg_set_variable_timestep": (_I32, [_P, _D, _D, _D]),
+    "mg_clock": (_I32, [_P, _P, _P, _P]),
+    "mg_dt_history": (_I32, [_P, _P, _I64, _P]),
     "mg_prepare": (_I32, [_P]),
     "mg_simulate": (_I32, [_P, _I64, _I32]),
     "mg_phase": (_I32, [_P, _I32]),
@@ -89,6 +92,12 @@ _PROTOS = {
     "mg_kernel_times": (_I32, [_P, _P, _I32, _P, _P]),
     "mg_launches_per_step": (_I32, [_P, _P]),
     "mg_stream": (_P, [_P]),
+    "mg_batch_create": (_I32, [_P, _I32, _I32, _P]),
+    "mg_batch_run": (_I32, [_P, _I64, _I32]),
+    "mg_batch_launches_per_step": (_I32, [_P, _P]),
+    "mg_batch_stream": (_P, [_P]),
+    "mg_batch_last_error": (ctypes.c_char_p, [_P]),
+    "mg_batch_destroy": (_I32, [_P]),
     "mg_host_register": (_I32, [_P, _U64]),
     "mg_host_unregister": (_I32, [_P]),
     "mg_mvv_noalloc": (_I32, [_P, _P, _P, _P, _I64, _P, _P]),
@@ -219,6 +228,24 @@ class Context:
     def set_timestep(self, dt):
         self._check(self.lib.mg_set_timestep(self.h, float(dt)))
 
+    def set_variable_timestep(self, dx_max, dt_min, dt_max):
+        """dt = clamp(dx_max / max|v|, dt_min, dt_max) before every step (Angstrom, ps)."""
+        self._check(self.lib.mg_set_variable_timestep(self.h, float(dx_max), float(dt_min), float(dt_max)))
+
+    def clock(self):
+        """(steps taken, simulated time in ps, dt of the last step)."""
+        n = ctypes.c_int64(0)
+        t = ctypes.c_double(0)
+        d = ctypes.c_double(0)
+        self._check(self.lib.mg_clock(self.h, ctypes.byref(n), ctypes.byref(t), ctypes.byref(d)))
+        return n.value, t.value, d.value
+
+    def dt_history(self, cap=65536):
+        out = np.zeros(cap)
+        n = ctypes.c_int64(0)
+        self._check(self.lib.mg_dt_history(self.h, out.ctypes.data_as(ctypes.c_void_p), cap, ctypes.byref(n)))
+        return out[: n.value].copy()
+
     def set_precision(self, precision):
         self._check(self.lib.mg_set_precision(self.h, PREC[precision]))
         self.precision = precision
@@ -335,6 +362,45 @@ class Context:
 
     def stream(self):
         return self.lib.mg_stream(self.h)
+
+
+class Batch:
+    """Independent replicas advanced together by one CUDA graph (mg_batch_*). The contexts must be
+    prepared and stay open while the batch exists."""
+
+    def __init__(self, contexts, steps_per_launch=1):
+        self.lib = load_library()
+        self.contexts = list(contexts)
+        arr = (ctypes.c_void_p * len(self.contexts))(*[c.h.value for c in self.contexts])
+        h = ctypes.c_void_p()
+        st = self.lib.mg_batch_create(arr, len(self.contexts), int(steps_per_launch), ctypes.byref(h))
+        if st != 0:
+            raise MgError(st, (self.lib.mg_batch_last_error(None) or b"").decode())
+        self.h = h
+
+    def run(self, steps, sync=True):
+        st = self.lib.mg_batch_run(self.h, int(steps), 1 if sync else 0)
+        if st != 0:
+            raise MgError(st, (self.lib.mg_batch_last_error(self.h) or b"").decode())
+
+    def launches_per_step(self):
+        n = ctypes.c_int32()
+        self.lib.mg_batch_launches_per_step(self.h, ctypes.byref(n))
+        return n.value
+
+    def stream(self):
+        return self.lib.mg_batch_stream(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Simulation:

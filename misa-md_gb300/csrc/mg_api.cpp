@@ -2,11 +2,14 @@
 // sequence (captured once as a CUDA graph), the reference's per-phase hooks and the thermo reductions.
 // The call order of one step follows simulation::simulate (src/simulation.cpp:238-268).
 
+#include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <string>
 #include <array>
+#include <mutex>
 #include <vector>
 
 #include "mg_internal.h"
@@ -43,11 +46,14 @@ struct mg_context {
     void *pot_mem = nullptr;
     OffsetTable offs;
     std::vector<int> lat_order[2];  // reordered full table (pruned entries first), linear offsets
+    NeighTables nt{};               // the tables as the kernels receive them
     int n_full = 0, n_pruned = 0;
     cudaStream_t stream = nullptr;
     int num_sms = 1;
-    StepParams sp{};
-    double dt = 0.0;
+    StepParams *d_sp = nullptr;     // device-resident step parameters and dt history
+    double dt = 0.0;                // fixed timestep (ps)
+    double dx_max = 0.0, dt_min = 0.0, dt_max = 0.0;  // variable timestep rule; dx_max <= 0: fixed
+    bool vmax_stale = true;         // velocities changed outside a kick: recompute max |v| first
     bool prepared = false;
     std::string err;
     mg_atom_element *d_aos = nullptr;
@@ -59,7 +65,8 @@ struct mg_context {
     uint32_t *d_ws_flags = nullptr;
     int64_t ws_cap = 0;
     cudaGraphExec_t graph_exec = nullptr;
-    double graph_dt = -1.0;
+    bool graph_stale = true;
+    uint64_t gen = 1;               // bumped whenever captured graphs of this context go stale
     int graph_prec = -1;
     int launches_per_step = 0;
     bool timing = false;
@@ -71,6 +78,7 @@ struct mg_context {
     int tune[2][2][2] = {{{0, 256}, {0, 256}}, {{0, 256}, {0, 256}}};  // [precision][rho, force] = {order, block}
     LaunchCtx lc() const {
         LaunchCtx l{stream, num_sms};
+        l.nt = &nt;
         l.rho_order = tune[precision][0][0];
         l.rho_block = tune[precision][0][1];
         l.force_order = tune[precision][1][0];
@@ -117,14 +125,14 @@ mg_status check_launch(mg_context *ctx) {
     return MG_OK;
 }
 
-void set_dt(mg_context *ctx, double dt) {  // NewtonMotion::preComputeDtInv2m (src/newton_motion.cpp:19-28)
+// NewtonMotion::setTimestepLength + preComputeDtInv2m (src/newton_motion.cpp:13-28), on the device
+// record; dx_max > 0 switches to the variable rule, which the step head applies from the next step
+void set_dt(mg_context *ctx, double dt, double dx_max = 0.0, double dt_min = 0.0, double dt_max = 0.0) {
     ctx->dt = dt;
-    ctx->sp.dt = dt;
-    for (int i = 0; i < 3; i++) {
-        const double m = atom_mass(i);
-        const double dt_halve = 0.5 * dt * kFtm2v;
-        ctx->sp.dt_inv_m[i] = dt_halve / m;
-    }
+    ctx->dx_max = dx_max;
+    ctx->dt_min = dt_min;
+    ctx->dt_max = dt_max;
+    launch_set_step(ctx->lc(), ctx->d_sp, dt, dx_max, dt_min, dt_max);
 }
 
 // timer helpers (direct launches only)
@@ -140,9 +148,9 @@ struct Timer {
 // ---- the kernel sequences ----
 void seq_firststep(mg_context *ctx, bool decide, Timer *t) {
     const LaunchCtx lc = ctx->lc();
-    launch_firststep(lc, ctx->g, ctx->s, ctx->in, ctx->sp, decide, ctx->mixed());
+    launch_firststep(lc, ctx->g, ctx->s, ctx->in, ctx->d_sp, decide, ctx->mixed());
     if (t) t->mark(1);
-    launch_inter_firststep(lc, ctx->in, ctx->sp);
+    launch_inter_firststep(lc, ctx->in, ctx->d_sp);
     if (t) t->mark(2);
 }
 void seq_compute_eam(mg_context *ctx, bool kick, bool with_manage_prefix, int manage_mask, Timer *t) {
@@ -161,20 +169,21 @@ void seq_compute_eam(mg_context *ctx, bool kick, bool with_manage_prefix, int ma
     if (t) t->mark(7);
     launch_ghost_df(lc, ctx->g, ctx->s, ctx->in, mx);
     if (t) t->mark(8);
-    launch_lat_force(lc, ctx->g, ctx->s, ctx->in, ctx->pt, ctx->sp, kick, mx, false);
+    launch_lat_force(lc, ctx->g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, kick, mx, false);
     if (t) t->mark(9);
     launch_inter_force(lc, ctx->g, ctx->s, ctx->in, ctx->pt, mx);
     if (t) t->mark(10);
-    if (kick) launch_secondstep(lc, ctx->g, ctx->s, ctx->in, ctx->sp, false);
+    if (kick) launch_secondstep(lc, ctx->g, ctx->s, ctx->in, ctx->d_sp, false);
     if (t) t->mark(11);
 }
 // one loop body: firststep, decide, exchangeInter, borderInter, exchangeAtom, computeEam, secondstep
 void seq_step(mg_context *ctx, Timer *t) {
     if (t) t->mark(0);
+    launch_step_head(ctx->lc(), ctx->d_sp);
     seq_firststep(ctx, true, t);
     seq_compute_eam(ctx, true, true, MANAGE_DECIDE | MANAGE_CLEAR_GHOST | MANAGE_EXCHANGE | MANAGE_BORDER, t);
 }
-constexpr int kLaunchesPerStep = 14;
+constexpr int kLaunchesPerStep = 12;
 
 mg_status require_ready(mg_context *ctx) {
     if (!ctx->pot_ready) { ctx->err = "potential not initialised"; return MG_ERR_POTENTIAL; }
@@ -189,37 +198,32 @@ mg_status ensure_aos(mg_context *ctx) {
 
 mg_status upload_tables(mg_context *ctx) {
     const int n = ctx->n_full;
-    std::vector<int> fe(n), fo(n);
-    for (int i = 0; i < n; i++) {
-        fe[i] = static_cast<int>(ctx->offs.off[0][i]);
-        fo[i] = static_cast<int>(ctx->offs.off[1][i]);
-    }
+    NeighTables &nt = ctx->nt;
+    std::memset(&nt, 0, sizeof(nt));
+    nt.nfull = n;
+    nt.npruned = ctx->n_pruned;
     // gather order (pruned entries first): linear offsets, parity-split index deltas, and the site
     // vectors in units of a0/2 (2 * the vector in units of a0: small exact integers)
-    std::vector<int> lat[2], lats[2];
-    std::vector<float> ds[2];
     const int64_t half = ctx->g.half;
     for (int p = 0; p < 2; p++) {
-        lat[p].resize(n);
-        lats[p].resize(n);
-        ds[p].resize(3 * n);
         for (int q = 0; q < n; q++) {
+            nt.full[p][q] = static_cast<int>(ctx->offs.off[p][q]);
             const int e = ctx->lat_order[p][q];
             const int64_t o = ctx->offs.off[p][e];
-            lat[p][q] = static_cast<int>(o);
+            nt.lat[p][q] = static_cast<int>(o);
             // slot s = 2k + p maps to p * half + k; its neighbour s + o has parity p2 and
             // (s + o) >> 1 = k + floor((p + o) / 2)
             const int64_t po = p + o;
             const int64_t p2 = ((po % 2) + 2) % 2;
             const int64_t fl = po >= 0 ? po / 2 : -((-po + 1) / 2);
-            lats[p][q] = static_cast<int>((p2 - p) * half + fl);
-            for (int k = 0; k < 3; k++) ds[p][3 * q + k] = static_cast<float>(2.0 * ctx->offs.vec[p][3 * e + k]);
+            nt.lats[p][q] = static_cast<int>((p2 - p) * half + fl);
+            const double *v = &ctx->offs.vec[p][3 * e];
+            nt.dsite[p][q] = make_float4((float) (2.0 * v[0]), (float) (2.0 * v[1]), (float) (2.0 * v[2]), 0.f);
         }
     }
-    set_constant_tables(fe.data(), fo.data(), n, lat[0].data(), lat[1].data(), lats[0].data(), lats[1].data(),
-                        ctx->n_pruned, ds[0].data(), ds[1].data(), ctx->stream);
+    set_mass_table(ctx->stream);
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) { ctx->err = std::string("constant tables: ") + cudaGetErrorString(e); return MG_ERR_CUDA; }
+    if (e != cudaSuccess) { ctx->err = std::string("mass table: ") + cudaGetErrorString(e); return MG_ERR_CUDA; }
     return MG_OK;
 }
 
@@ -283,7 +287,8 @@ mg_status install_potential(mg_context *ctx, const HostPotential &hp) {
     pt.z_vf = d_vf + base_z; pt.z_dff = d_df + base_z;
     ctx->hp = hp;
     ctx->pot_ready = true;
-    ctx->graph_dt = -1.0;  // rebuild graphs
+    ctx->graph_stale = true;
+    ctx->gen++;  // rebuild graphs
     return MG_OK;
 }
 
@@ -297,7 +302,7 @@ mg_status check_types(mg_context *ctx, const mg_atom_element *atoms, int64_t n) 
 }
 
 mg_status build_graph(mg_context *ctx) {
-    if (ctx->graph_exec && ctx->graph_dt == ctx->dt && ctx->graph_prec == ctx->precision) return MG_OK;
+    if (ctx->graph_exec && !ctx->graph_stale && ctx->graph_prec == ctx->precision) return MG_OK;
     if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
     cudaGraph_t graph;
     MG_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
@@ -309,7 +314,7 @@ mg_status build_graph(mg_context *ctx) {
     cudaError_t e = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) { ctx->err = std::string("graph instantiate: ") + cudaGetErrorString(e); return MG_ERR_CUDA; }
-    ctx->graph_dt = ctx->dt;
+    ctx->graph_stale = false;
     ctx->graph_prec = ctx->precision;
     return MG_OK;
 }
@@ -450,6 +455,7 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     ctx->n_partials = ctx->num_sms * 4;
     ALLOC(ctx->d_partials, (size_t) ctx->n_partials * 8);
     ALLOC(ctx->d_thermo, 8);
+    ALLOC(ctx->d_sp, 1);
 #undef ALLOC
     e = cudaMemsetAsync(in.cnt, 0, CNT_WORDS * sizeof(int), ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(in.claim, 0x7f, ns * sizeof(int), ctx->stream);  // 0x7f7f7f7f > any list index
@@ -457,6 +463,7 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     if (e == cudaSuccess) e = cudaMemsetAsync(in.n_bucket, 0, sizeof(int), ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s.type, 0xff, ns, ctx->stream);  // all slots INVALID
     if (e == cudaSuccess) e = cudaMemsetAsync(s.u4, 0xff, ns * sizeof(float4), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_sp, 0, sizeof(StepParams), ctx->stream);
     if (e != cudaSuccess) return fail(e);
     if (upload_tables(ctx) != MG_OK) { g_create_error = ctx->err; mg_destroy(ctx); return MG_ERR_CUDA; }
     set_dt(ctx, 0.001);
@@ -487,6 +494,7 @@ mg_status mg_set_precision(mg_context *ctx, int32_t precision) {
     if (!ctx || (precision != MG_PREC_FP64 && precision != MG_PREC_MIXED)) return MG_ERR_ARG;
     ctx->precision = precision;
     ctx->prepared = false;  // derived arrays (u4, df32) must be rebuilt by an upload
+    ctx->gen++;
     return MG_OK;
 }
 
@@ -560,6 +568,7 @@ static mg_status hook_upload(mg_context *ctx, mg_atom_element *atoms, double cut
     MG_CK(cudaMemcpyAsync(ctx->d_aos, atoms, sizeof(mg_atom_element) * ctx->g.n_slots, cudaMemcpyHostToDevice, ctx->stream));
     launch_unpack_aos(ctx->lc(), ctx->g, ctx->d_aos, ctx->s, ctx->in, ctx->types_ok_mask, ctx->mixed());
     launch_far_rebuild(ctx->lc(), ctx->g, ctx->s, ctx->in);
+    ctx->vmax_stale = true;
     return check_launch(ctx);
 }
 static mg_status hook_download(mg_context *ctx, mg_atom_element *atoms, int fields) {
@@ -587,8 +596,7 @@ mg_status mg_eam_df_calc(mg_context *ctx, mg_atom_element *atoms, double cutoff_
 mg_status mg_eam_force_calc(mg_context *ctx, mg_atom_element *atoms, double cutoff_radius) {
     mg_status st = hook_upload(ctx, atoms, cutoff_radius);
     if (st != MG_OK) return st;
-    StepParams none{};
-    launch_lat_force(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, none, false, ctx->mixed(), true);
+    launch_lat_force(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, false, ctx->mixed(), true);
     return hook_download(ctx, atoms, PACK_F);
 }
 
@@ -627,6 +635,7 @@ mg_status mg_upload(mg_context *ctx, const mg_atom_element *atoms, int64_t n_slo
     launch_set_counts(ctx->lc(), ctx->in, static_cast<int>(n_inter));
     launch_far_rebuild(ctx->lc(), ctx->g, ctx->s, ctx->in);
     ctx->prepared = false;
+    ctx->vmax_stale = true;
     ctx->energy_valid = false;
     return check_launch(ctx);
 }
@@ -700,6 +709,48 @@ mg_status mg_download_ghost_inter(mg_context *ctx, mg_atom_element *ghost, int64
 mg_status mg_set_timestep(mg_context *ctx, double dt) {
     if (!ctx || !(dt > 0)) return MG_ERR_ARG;
     set_dt(ctx, dt);
+    return check_launch(ctx);
+}
+
+mg_status mg_set_variable_timestep(mg_context *ctx, double dx_max, double dt_min, double dt_max) {
+    if (!ctx) return MG_ERR_ARG;
+    if (!(dx_max > 0) || !(dt_min > 0) || !(dt_max >= dt_min) || !std::isfinite(dt_max) || !std::isfinite(dx_max)) {
+        ctx->err = "variable timestep needs dx_max > 0 and 0 < dt_min <= dt_max (finite)";
+        return MG_ERR_ARG;
+    }
+    set_dt(ctx, dt_max, dx_max, dt_min, dt_max);
+    return check_launch(ctx);
+}
+
+mg_status mg_clock(mg_context *ctx, int64_t *steps, double *time_ps, double *dt_ps) {
+    if (!ctx) return MG_ERR_ARG;
+    StepParams head;
+    MG_CK(cudaMemcpyAsync(&head, ctx->d_sp, offsetof(StepParams, vmax2), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_CK(cudaStreamSynchronize(ctx->stream));
+    if (steps) *steps = head.steps;
+    if (time_ps) *time_ps = head.time;
+    if (dt_ps) *dt_ps = head.dt;
+    return MG_OK;
+}
+
+mg_status mg_dt_history(mg_context *ctx, double *out, int64_t cap, int64_t *n_out) {
+    if (!ctx || cap < 0 || (cap > 0 && !out) || !n_out) return MG_ERR_ARG;
+    int64_t steps = 0;
+    mg_status st = mg_clock(ctx, &steps, nullptr, nullptr);
+    if (st != MG_OK) return st;
+    const int64_t n = std::min<int64_t>(std::min<int64_t>(steps, cap), kDtHistory);
+    const double *hist = reinterpret_cast<const double *>(reinterpret_cast<const char *>(ctx->d_sp) + offsetof(StepParams, hist));
+    // the last n steps in order: steps - n .. steps - 1, in at most two runs of the ring
+    const int64_t first = steps - n;
+    int64_t done = 0;
+    while (done < n) {
+        const int64_t at = (first + done) % kDtHistory;
+        const int64_t run = std::min<int64_t>(n - done, kDtHistory - at);
+        MG_CK(cudaMemcpyAsync(out + done, hist + at, run * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        done += run;
+    }
+    MG_CK(cudaStreamSynchronize(ctx->stream));
+    *n_out = n;
     return MG_OK;
 }
 
@@ -721,6 +772,10 @@ mg_status mg_simulate(mg_context *ctx, int64_t nsteps, int32_t sync) {
     if (!ctx || nsteps < 0) return MG_ERR_ARG;
     if (!ctx->prepared) { ctx->err = "mg_prepare must run before mg_simulate"; return MG_ERR_STATE; }
     mg_status st;
+    if (ctx->vmax_stale) {
+        launch_vmax_full(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->d_sp);
+        ctx->vmax_stale = false;
+    }
     if (ctx->timing) {
         const size_t need = static_cast<size_t>(nsteps) * (kNumTimers + 1);
         while (ctx->ev.size() < need) {
@@ -771,12 +826,13 @@ mg_status mg_phase(mg_context *ctx, int32_t phase) {
         case 3: launch_inter_manage(lc, ctx->g, ctx->s, ctx->in, MANAGE_BORDER, ctx->mixed()); break;
         case 4: launch_ghost_copy(lc, ctx->g, ctx->s, ctx->mixed()); break;
         case 5: seq_compute_eam(ctx, false, false, 0, nullptr); break;
-        case 6: launch_secondstep(lc, ctx->g, ctx->s, ctx->in, ctx->sp, true); break;
+        case 6: launch_secondstep(lc, ctx->g, ctx->s, ctx->in, ctx->d_sp, true); break;
     }
     if ((st = check_launch(ctx)) != MG_OK) return st;
     uint32_t bits = 0;
     if ((st = read_device_errors(ctx, &bits)) != MG_OK) return st;
     ctx->energy_valid = false;
+    ctx->vmax_stale = true;
     return status_from_bits(ctx, bits);
 }
 
@@ -791,6 +847,7 @@ mg_status mg_collision_step(mg_context *ctx, const int32_t lat[4], const double 
         const int64_t kk = ((int64_t) (lat[2] + g.gz) * g.Sy + (lat[1] + g.gy)) * g.Sx + (lat[0] * 2 + g.gx) + lat[3];
         if (kk < 0 || kk >= g.n_slots) { ctx->err = "PKA slot outside the grid"; return MG_ERR_ARG; }
         launch_setv(ctx->lc(), g, ctx->s, kk, dir, energy);
+        ctx->vmax_stale = true;
     }
     // exchangeInter, borderInter (the ghost list is not cleared here, as in the reference),
     // exchangeAtom, clearForce, computeEam (src/simulation.cpp:282-291)
@@ -807,6 +864,7 @@ mg_status mg_rescale(mg_context *ctx, double t_set, uint64_t n_atoms) {
     if (!ctx || n_atoms < 2) return MG_ERR_ARG;
     launch_thermo(ctx->lc(), ctx->g, ctx->s, ctx->in, false, ctx->d_partials, ctx->n_partials, ctx->d_thermo);
     launch_rescale(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->d_thermo, t_set, n_atoms);
+    ctx->vmax_stale = true;
     mg_status st = check_launch(ctx);
     if (st != MG_OK) return st;
     MG_CK(cudaStreamSynchronize(ctx->stream));
@@ -912,6 +970,7 @@ struct TuneKey {
     }
 };
 std::vector<std::pair<TuneKey, std::array<int, 4>>> g_tune_cache;
+std::mutex g_tune_mutex;
 }  // namespace
 
 mg_status mg_autotune(mg_context *ctx, int32_t reps, int32_t out[4]) {
@@ -919,12 +978,16 @@ mg_status mg_autotune(mg_context *ctx, int32_t reps, int32_t out[4]) {
     if (!ctx->prepared) { ctx->err = "mg_prepare must run before mg_autotune"; return MG_ERR_STATE; }
     const int p = ctx->precision;
     const TuneKey key{{ctx->g.cells[0], ctx->g.cells[1], ctx->g.cells[2]}, p};
-    for (auto &kv : g_tune_cache) {
-        if (kv.first == key) {
-            for (int k = 0; k < 2; k++) { ctx->tune[p][k][0] = kv.second[2 * k]; ctx->tune[p][k][1] = kv.second[2 * k + 1]; }
-            if (out) for (int k = 0; k < 4; k++) out[k] = kv.second[k];
-            ctx->graph_dt = -1.0;
-            return MG_OK;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        for (auto &kv : g_tune_cache) {
+            if (kv.first == key) {
+                for (int k = 0; k < 2; k++) { ctx->tune[p][k][0] = kv.second[2 * k]; ctx->tune[p][k][1] = kv.second[2 * k + 1]; }
+                if (out) for (int k = 0; k < 4; k++) out[k] = kv.second[k];
+                ctx->graph_stale = true;
+                ctx->gen++;
+                return MG_OK;
+            }
         }
     }
     if (reps < 1) reps = 3;
@@ -933,7 +996,6 @@ mg_status mg_autotune(mg_context *ctx, int32_t reps, int32_t out[4]) {
     MG_CK(cudaEventCreate(&e1));
     const int blocks[3] = {128, 256, 512};
     std::array<int, 4> best{};
-    StepParams none{};
     for (int kern = 0; kern < 2; kern++) {
         float best_ms = 1e30f;
         for (int order = 0; order < 2; order++) {
@@ -943,7 +1005,7 @@ mg_status mg_autotune(mg_context *ctx, int32_t reps, int32_t out[4]) {
                 const LaunchCtx lc = ctx->lc();
                 auto run = [&]() {
                     if (kern == 0) launch_lat_rho(lc, ctx->g, ctx->s, ctx->in, ctx->pt, ctx->mixed(), false);
-                    else launch_lat_force(lc, ctx->g, ctx->s, ctx->in, ctx->pt, none, false, ctx->mixed(), false);
+                    else launch_lat_force(lc, ctx->g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, false, ctx->mixed(), false);
                 };
                 run();  // warm
                 cudaEventRecord(e0, ctx->stream);
@@ -962,9 +1024,13 @@ mg_status mg_autotune(mg_context *ctx, int32_t reps, int32_t out[4]) {
     cudaEventDestroy(e1);
     mg_status st = check_launch(ctx);
     if (st != MG_OK) return st;
-    g_tune_cache.push_back({key, best});
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tune_cache.push_back({key, best});
+    }
     if (out) for (int k = 0; k < 4; k++) out[k] = best[k];
-    ctx->graph_dt = -1.0;  // the captured graph holds the old launch shapes
+    ctx->graph_stale = true;
+    ctx->gen++;  // the captured graph holds the old launch shapes
     return MG_OK;
 }
 
@@ -976,7 +1042,8 @@ mg_status mg_set_tuning(mg_context *ctx, const int32_t tune[4]) {
         ctx->tune[ctx->precision][k][0] = order;
         ctx->tune[ctx->precision][k][1] = b;
     }
-    ctx->graph_dt = -1.0;
+    ctx->graph_stale = true;
+    ctx->gen++;
     return MG_OK;
 }
 
@@ -1003,6 +1070,180 @@ mg_status mg_launches_per_step(const mg_context *ctx, int32_t *n) {
 }
 
 void *mg_stream(const mg_context *ctx) { return ctx ? (void *) ctx->stream : nullptr; }
+
+// ---------------------------------------------------------------------------------------------
+// batched independent replicas (extension: many cascades advanced by one graph launch)
+// ---------------------------------------------------------------------------------------------
+struct mg_batch {
+    std::vector<mg_context *> ctxs;
+    std::vector<uint64_t> gens;          // each context's generation when the graphs were captured
+    int steps_per_launch = 1;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t exec_k = nullptr;    // steps_per_launch loop bodies of every replica
+    cudaGraphExec_t exec_1 = nullptr;    // one loop body of every replica (remainders)
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    std::vector<cudaEvent_t> ev_ctx;
+    int launches_per_step = 0;
+    std::string err;
+};
+
+namespace {
+
+#define MB_CK(call)                                                                             \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess) {                                                                \
+            b->err = std::string(#call) + ": " + cudaGetErrorString(e_);                       \
+            return MG_ERR_CUDA;                                                                 \
+        }                                                                                       \
+    } while (0)
+
+// Fork/join capture: every replica's stream joins the batch stream's capture, records `steps`
+// loop bodies, and the batch stream joins them all at the end. The replicas share no memory, so
+// the graph holds one independent branch per replica.
+mg_status capture_batch(mg_batch *b, int steps, cudaGraphExec_t *exec, int *n_nodes) {
+    cudaGraph_t graph = nullptr;
+    MB_CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaEventRecord(b->ev_fork, b->stream);
+    for (size_t r = 0; r < b->ctxs.size() && e == cudaSuccess; r++) {
+        mg_context *ctx = b->ctxs[r];
+        e = cudaStreamWaitEvent(ctx->stream, b->ev_fork, 0);
+        for (int k = 0; k < steps && e == cudaSuccess; k++) {
+            seq_step(ctx, nullptr);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(b->ev_ctx[r], ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->ev_ctx[r], 0);
+    }
+    const cudaError_t e_end = cudaStreamEndCapture(b->stream, &graph);
+    if (e != cudaSuccess || e_end != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        b->err = std::string("batch capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e_end);
+        return MG_ERR_CUDA;
+    }
+    size_t nn = 0;
+    cudaGraphGetNodes(graph, nullptr, &nn);
+    *n_nodes = static_cast<int>(nn);
+    e = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { b->err = std::string("batch graph instantiate: ") + cudaGetErrorString(e); return MG_ERR_CUDA; }
+    return MG_OK;
+}
+
+mg_status batch_capture_all(mg_batch *b) {
+    if (b->exec_k) { cudaGraphExecDestroy(b->exec_k); b->exec_k = nullptr; }
+    if (b->exec_1) { cudaGraphExecDestroy(b->exec_1); b->exec_1 = nullptr; }
+    for (mg_context *ctx : b->ctxs) MB_CK(cudaStreamSynchronize(ctx->stream));
+    int nk = 0, n1 = 0;
+    mg_status st = capture_batch(b, b->steps_per_launch, &b->exec_k, &nk);
+    if (st == MG_OK && b->steps_per_launch > 1) st = capture_batch(b, 1, &b->exec_1, &n1);
+    if (st != MG_OK) return st;
+    b->launches_per_step = b->steps_per_launch > 1 ? n1 : nk;
+    for (size_t r = 0; r < b->ctxs.size(); r++) b->gens[r] = b->ctxs[r]->gen;
+    return MG_OK;
+}
+
+}  // namespace
+
+mg_status mg_batch_create(mg_context *const *ctxs, int32_t n, int32_t steps_per_launch, mg_batch **out) {
+    if (!ctxs || n < 1 || !out || steps_per_launch < 1) return MG_ERR_ARG;
+    for (int32_t r = 0; r < n; r++) {
+        if (!ctxs[r]) return MG_ERR_ARG;
+        for (int32_t q = 0; q < r; q++)
+            if (ctxs[q] == ctxs[r]) { g_create_error = "mg_batch_create: a context appears twice"; return MG_ERR_ARG; }
+        if (!ctxs[r]->prepared || !ctxs[r]->pot_ready) {
+            g_create_error = "mg_batch_create: replica " + std::to_string(r) + " is not prepared";
+            return MG_ERR_STATE;
+        }
+    }
+    auto *b = new mg_batch();
+    b->ctxs.assign(ctxs, ctxs + n);
+    b->gens.assign(n, 0);
+    b->steps_per_launch = steps_per_launch;
+    b->ev_ctx.assign(n, nullptr);
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
+    for (int32_t r = 0; r < n && e == cudaSuccess; r++) e = cudaEventCreateWithFlags(&b->ev_ctx[r], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        g_create_error = std::string("mg_batch_create: ") + cudaGetErrorString(e);
+        mg_batch_destroy(b);
+        return MG_ERR_CUDA;
+    }
+    if (batch_capture_all(b) != MG_OK) {
+        g_create_error = b->err;
+        mg_batch_destroy(b);
+        return MG_ERR_CUDA;
+    }
+    *out = b;
+    return MG_OK;
+}
+
+mg_status mg_batch_run(mg_batch *b, int64_t nsteps, int32_t sync) {
+    if (!b || nsteps < 0) return MG_ERR_ARG;
+    for (size_t r = 0; r < b->ctxs.size(); r++) {
+        if (!b->ctxs[r]->prepared) { b->err = "replica " + std::to_string(r) + " is not prepared"; return MG_ERR_STATE; }
+        if (b->ctxs[r]->gen != b->gens[r]) {  // precision, tuning or potential changed since the capture
+            mg_status st = batch_capture_all(b);
+            if (st != MG_OK) return st;
+            break;
+        }
+    }
+    // the batch runs after each replica's pending work, and each replica's later work after the batch
+    for (size_t r = 0; r < b->ctxs.size(); r++) {
+        mg_context *ctx = b->ctxs[r];
+        if (ctx->vmax_stale) {
+            launch_vmax_full(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->d_sp);
+            ctx->vmax_stale = false;
+        }
+        MB_CK(cudaEventRecord(b->ev_ctx[r], ctx->stream));
+        MB_CK(cudaStreamWaitEvent(b->stream, b->ev_ctx[r], 0));
+    }
+    const int64_t k = b->steps_per_launch;
+    for (int64_t i = 0; i < nsteps / k; i++) MB_CK(cudaGraphLaunch(b->exec_k, b->stream));
+    for (int64_t i = 0; i < nsteps % k; i++) MB_CK(cudaGraphLaunch(b->exec_1, b->stream));
+    MB_CK(cudaEventRecord(b->ev_join, b->stream));
+    for (mg_context *ctx : b->ctxs) {
+        MB_CK(cudaStreamWaitEvent(ctx->stream, b->ev_join, 0));
+        ctx->energy_valid = false;
+    }
+    if (!sync) return MG_OK;
+    MB_CK(cudaStreamSynchronize(b->stream));
+    for (size_t r = 0; r < b->ctxs.size(); r++) {
+        mg_context *ctx = b->ctxs[r];
+        uint32_t bits = 0;
+        mg_status st = read_device_errors(ctx, &bits);
+        if (st == MG_OK) st = status_from_bits(ctx, bits);
+        if (st != MG_OK) {
+            b->err = "replica " + std::to_string(r) + ": " + ctx->err;
+            return st;
+        }
+    }
+    return MG_OK;
+}
+
+mg_status mg_batch_launches_per_step(const mg_batch *b, int32_t *n) {
+    if (!b || !n) return MG_ERR_ARG;
+    *n = b->launches_per_step;
+    return MG_OK;
+}
+
+void *mg_batch_stream(const mg_batch *b) { return b ? (void *) b->stream : nullptr; }
+
+const char *mg_batch_last_error(const mg_batch *b) { return b ? b->err.c_str() : g_create_error.c_str(); }
+
+mg_status mg_batch_destroy(mg_batch *b) {
+    if (!b) return MG_ERR_ARG;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->exec_k) cudaGraphExecDestroy(b->exec_k);
+    if (b->exec_1) cudaGraphExecDestroy(b->exec_1);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_join) cudaEventDestroy(b->ev_join);
+    for (cudaEvent_t e : b->ev_ctx) if (e) cudaEventDestroy(e);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return MG_OK;
+}
 
 mg_status mg_host_register(void *ptr, uint64_t bytes) {
     if (!ptr || bytes == 0) return MG_ERR_ARG;

@@ -16,8 +16,7 @@ constexpr double kBoltz = 8.617343e-5;       // src/types/pre_define.h:11
 constexpr double kMvv2e = 1.0364269e-4;      // src/types/pre_define.h:18
 constexpr double kFtm2v = (1.0 / kMvv2e);    // src/types/pre_define.h:19
 constexpr double kNeiLatCutoff = 0.5;        // src/md_building_config.h.in:24
-constexpr int kMaxFull = 256;                // capacity of a full offset table per parity
-constexpr int kMaxPruned = 128;              // capacity of a pruned full table per parity
+constexpr int kMaxFull = 232;                // capacity of a full offset table per parity
 
 // box flags (src/lattice/box.h:12-20)
 constexpr uint32_t kInBox = 0, kXLow = 1u, kXHigh = 2u, kYLow = 4u, kYHigh = 8u, kZLow = 16u, kZHigh = 32u;
@@ -123,10 +122,20 @@ struct PotTables {
     const float4 *rho_vf, *rho_dff, *F_vf, *F_dff, *z_vf, *z_dff;
 };
 
-// Constant per-step parameters.
+// Per-step parameters, resident in device memory (one record per context). Kernels read dt and the
+// half-kick factors dt/(2m) from here, so a new timestep needs no new graph. In variable-timestep
+// mode the step-head kernel rewrites them every step from the largest speed the previous kick left.
+constexpr int kVmaxSlots = 1024;    // spread max-words: one per (warp index mod kVmaxSlots)
+constexpr int kDtHistory = 65536;   // ring of the most recent timesteps
 struct StepParams {
     double dt;
     double dt_inv_m[3];
+    double dx_max, dt_min, dt_max;  // variable timestep: dt = clamp(dx_max / max|v|, dt_min, dt_max); dx_max <= 0: fixed
+    double time;                    // simulated time (ps) summed over the steps taken
+    long long steps;                // steps taken since the context was created
+    long long pad_;
+    unsigned long long vmax2[kVmaxSlots];  // max |v|^2 of the last kick, bit patterns of non-negative doubles
+    double hist[kDtHistory];               // dt of step k (0-based) at hist[k % kDtHistory]
 };
 
 // Host-side spline (FP64 coefficients), built identically to the setfl interpolation scheme.
@@ -166,20 +175,28 @@ struct OffsetTable {
 };
 OffsetTable make_offsets(int64_t size_x, int64_t size_y, int cut_lattice, double rcf);
 
+// Neighbour offset tables of one slot grid, passed to the kernels by value as a __grid_constant__
+// parameter (13 KB, within the 32 KB parameter space): every context carries its own, and the
+// candidate loops read them as warp-uniform constant-bank loads.
+struct NeighTables {
+    int nfull, npruned;
+    int full[2][kMaxFull];      // reference order (inter-atom passes), linear slot offsets
+    int lat[2][kMaxFull];       // gather order: entries within rc + 0.4 a0 first; linear offsets
+    int lats[2][kMaxFull];      // gather order, parity-split index deltas
+    float4 dsite[2][kMaxFull];  // gather order, site_j - site_i in units of a0/2 (w unused)
+};
+
 // ---- kernel launchers (defined in the .cu files) ----
 struct LaunchCtx {
     cudaStream_t stream;
     int num_sms;
     int rho_order = 0, rho_block = 256;      // gather thread order and block size of the density pass
     int force_order = 0, force_block = 256;  // the same for the force pass (chosen by mg_autotune)
+    const NeighTables *nt = nullptr;         // the context's offset tables
 };
 
-// full: reference-order full tables (linear offsets); lat: the gather order (pruned entries first),
-// linear offsets; lats: the same entries as parity-split index deltas; dsite: their site vectors in
-// units of a0/2 (3 floats per entry).
-void set_constant_tables(const int *full_even, const int *full_odd, int n_full, const int *lat_even,
-                         const int *lat_odd, const int *lats_even, const int *lats_odd, int n_pruned,
-                         const float *dsite_even, const float *dsite_odd, cudaStream_t stream);
+// Mass table shared by all contexts (atom types are fixed).
+void set_mass_table(cudaStream_t stream);
 
 void launch_unpack_aos(const LaunchCtx &lc, const Geom &g, const mg_atom_element *aos, Slots s, Inter in, int types_ok_mask,
                        bool mixed);
@@ -188,15 +205,21 @@ void launch_set_counts(const LaunchCtx &lc, Inter in, int n_inter);
 void launch_pack_aos(const LaunchCtx &lc, const Geom &g, mg_atom_element *aos, Slots s, int fields, bool mixed);
 enum { PACK_ALL = 0xff, PACK_RHO = 1, PACK_DF = 2, PACK_F = 4 };
 
-void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams p, bool decide, bool mixed);
+void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const StepParams *sp, bool decide, bool mixed);
 void launch_decide_scan(const LaunchCtx &lc, const Geom &g, Slots s, Inter in);
 void launch_ghost_copy(const LaunchCtx &lc, const Geom &g, Slots s, bool mixed);
 void launch_ghost_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool mixed);
 void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook);
 void launch_lat_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook);
-void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams p, bool kick,
+void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *sp, bool kick,
                       bool mixed, bool hook);
-void launch_secondstep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams p, bool lattice);
+void launch_secondstep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams *sp, bool lattice);
+// step head: records the step's dt and, in variable mode, sets dt from the last kick's max |v|
+void launch_step_head(const LaunchCtx &lc, StepParams *sp);
+// set the timestep rule and dt / dt/(2m) (dx_max <= 0: fixed dt)
+void launch_set_step(const LaunchCtx &lc, StepParams *sp, double dt, double dx_max, double dt_min, double dt_max);
+// recompute the max |v|^2 words from the state (after uploads, setv, rescale, single phases)
+void launch_vmax_full(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams *sp);
 void launch_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed);
 // far atoms: rebuild the list and its neighbourhood marks from positions (uploads, hooks)
 void launch_far_rebuild(const LaunchCtx &lc, const Geom &g, Slots s, Inter in);
@@ -205,7 +228,7 @@ enum { MANAGE_DECIDE = 1, MANAGE_CLEAR_GHOST = 2, MANAGE_EXCHANGE = 4, MANAGE_BO
 void launch_inter_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed);
 void launch_inter_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed);
 void launch_inter_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed);
-void launch_inter_firststep(const LaunchCtx &lc, Inter in, StepParams p);
+void launch_inter_firststep(const LaunchCtx &lc, Inter in, const StepParams *sp);
 void launch_setv(const LaunchCtx &lc, const Geom &g, Slots s, int64_t slot, const double dir[3], double energy);
 void launch_rescale(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const double *d_factor_src, double t_set,
                     uint64_t n_atoms);

@@ -11,6 +11,7 @@
 // Wigner-Seitz mapping, ghost shifts and setv.
 
 #include <climits>
+#include <cstddef>
 #include <cstdio>
 
 #include "mg_internal.h"
@@ -20,43 +21,13 @@ namespace mg {
 // ------------------------------------------------------------------------------------------------
 // constant tables
 // ------------------------------------------------------------------------------------------------
-__constant__ int c_full[2][kMaxFull];       // reference full offset tables (linear, per parity)
-__constant__ int c_nfull;
-// Lattice gather tables: the full table reordered so that the entries whose sites are closer than
-// rc + 0.4 a0 come first (c_npruned of them). While every lattice atom is within 0.2 a0 of its site
-// (guaranteed after atom::decide, except for recombined "far" atoms) only those can hold a neighbour
-// inside the cutoff.
-__constant__ int c_lat[2][kMaxFull];        // linear slot offsets
-__constant__ int c_lats[2][kMaxFull];       // parity-split index deltas of the same entries
-__constant__ int c_npruned;
-__constant__ float4 c_dsite[2][kMaxFull];   // site_j - site_i of the entries, units a0/2 (w unused)
 __constant__ double c_mass[3];
 
-void set_constant_tables(const int *full_even, const int *full_odd, int n_full, const int *lat_even,
-                         const int *lat_odd, const int *lats_even, const int *lats_odd, int n_pruned,
-                         const float *dsite_even, const float *dsite_odd, cudaStream_t stream) {
-    static int full[2][kMaxFull];
-    static int lat[2][kMaxFull];
-    static int lats[2][kMaxFull];
-    static float4 dsite[2][kMaxFull];
-    for (int i = 0; i < n_full; i++) {
-        full[0][i] = full_even[i]; full[1][i] = full_odd[i];
-        lat[0][i] = lat_even[i]; lat[1][i] = lat_odd[i];
-        lats[0][i] = lats_even[i]; lats[1][i] = lats_odd[i];
-        dsite[0][i] = make_float4(dsite_even[3 * i], dsite_even[3 * i + 1], dsite_even[3 * i + 2], 0.f);
-        dsite[1][i] = make_float4(dsite_odd[3 * i], dsite_odd[3 * i + 1], dsite_odd[3 * i + 2], 0.f);
-    }
+void set_mass_table(cudaStream_t stream) {
     const double mass[3] = {atom_mass(0), atom_mass(1), atom_mass(2)};
-    cudaMemcpyToSymbolAsync(c_full, full, sizeof(full), 0, cudaMemcpyHostToDevice, stream);
-    cudaMemcpyToSymbolAsync(c_nfull, &n_full, sizeof(int), 0, cudaMemcpyHostToDevice, stream);
-    cudaMemcpyToSymbolAsync(c_lat, lat, sizeof(lat), 0, cudaMemcpyHostToDevice, stream);
-    cudaMemcpyToSymbolAsync(c_lats, lats, sizeof(lats), 0, cudaMemcpyHostToDevice, stream);
-    cudaMemcpyToSymbolAsync(c_npruned, &n_pruned, sizeof(int), 0, cudaMemcpyHostToDevice, stream);
-    cudaMemcpyToSymbolAsync(c_dsite, dsite, sizeof(dsite), 0, cudaMemcpyHostToDevice, stream);
     cudaMemcpyToSymbolAsync(c_mass, mass, sizeof(mass), 0, cudaMemcpyHostToDevice, stream);
     cudaStreamSynchronize(stream);
 }
-
 
 // ------------------------------------------------------------------------------------------------
 // index helpers
@@ -170,8 +141,26 @@ __device__ __forceinline__ float4 make_u4(const Geom &g, double x, double y, dou
                        __double2float_rn(__dmul_rn(__dsub_rn(z, zs), g.inv_h)), __int_as_float(type));
 }
 
-__device__ __forceinline__ double dt_inv_m_of(const StepParams &p, int type) {
-    return type == 0 ? p.dt_inv_m[0] : (type == 1 ? p.dt_inv_m[1] : p.dt_inv_m[2]);
+__device__ __forceinline__ double dt_inv_m_of(const StepParams *p, int type) {
+    return type == 0 ? p->dt_inv_m[0] : (type == 1 ? p->dt_inv_m[1] : p->dt_inv_m[2]);
+}
+// |v|^2 in the order the oracle computes it ((vx^2 + vy^2) + vz^2, each operation rounded)
+__device__ __forceinline__ double speed2(double vx, double vy, double vz) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz));
+}
+// Max of v2 over the lanes that call this together, then one atomicMax per such group into a word
+// picked by the warp's index, so the words see few atomics each. Non-negative doubles order like
+// their bit patterns, so the max is taken on the 64-bit patterns, high word first.
+__device__ __forceinline__ void note_vmax2(StepParams *sp, double v2) {
+    const unsigned mask = __activemask();
+    const unsigned long long b = (unsigned long long) __double_as_longlong(v2);
+    const unsigned hi = (unsigned) (b >> 32), lo = (unsigned) b;
+    const unsigned mhi = __reduce_max_sync(mask, hi);
+    const unsigned mlo = __reduce_max_sync(mask, hi == mhi ? lo : 0u);
+    if ((threadIdx.x & 31) == (unsigned) (__ffs(mask) - 1)) {
+        const int w = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) & (kVmaxSlots - 1);
+        atomicMax(&sp->vmax2[w], ((unsigned long long) mhi << 32) | mlo);
+    }
 }
 __device__ __forceinline__ void set_error(Inter &in, uint32_t bit) { atomicOr((unsigned *) &in.cnt[CNT_ERRORS], bit); }
 // Lattice passes can fuse df / the half-kick only when no other kernel adds density or force to
@@ -310,7 +299,7 @@ void launch_pack_aos(const LaunchCtx &lc, const Geom &g, mg_atom_element *aos, S
 // sorts them into the reference's k, j, i scan order.
 // ------------------------------------------------------------------------------------------------
 template <bool MOVE, bool DECIDE, bool MIXED>
-__global__ void __launch_bounds__(256) k_firststep(Geom g, Slots s, Inter in, StepParams p) {
+__global__ void __launch_bounds__(256) k_firststep(Geom g, Slots s, Inter in, const StepParams *__restrict__ p) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= g.n_local) return;
     int i, j, k;
@@ -324,9 +313,10 @@ __global__ void __launch_bounds__(256) k_firststep(Geom g, Slots s, Inter in, St
         vx = __dadd_rn(vx, __dmul_rn(c, s.fx[sl]));
         vy = __dadd_rn(vy, __dmul_rn(c, s.fy[sl]));
         vz = __dadd_rn(vz, __dmul_rn(c, s.fz[sl]));
-        x = __dadd_rn(x, __dmul_rn(p.dt, vx));
-        y = __dadd_rn(y, __dmul_rn(p.dt, vy));
-        z = __dadd_rn(z, __dmul_rn(p.dt, vz));
+        const double dt = p->dt;
+        x = __dadd_rn(x, __dmul_rn(dt, vx));
+        y = __dadd_rn(y, __dmul_rn(dt, vy));
+        z = __dadd_rn(z, __dmul_rn(dt, vz));
         s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz;
         s.x[sl] = x; s.y[sl] = y; s.z[sl] = z;
     }
@@ -351,7 +341,7 @@ __global__ void __launch_bounds__(256) k_firststep(Geom g, Slots s, Inter in, St
     }
 }
 
-void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams p, bool decide, bool mixed) {
+void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const StepParams *p, bool decide, bool mixed) {
     const int b = 256, n = (g.n_local + b - 1) / b;
     if (mixed) {
         if (decide) k_firststep<true, true, true><<<n, b, 0, lc.stream>>>(g, s, in, p);
@@ -363,24 +353,24 @@ void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, Ste
 }
 void launch_decide_scan(const LaunchCtx &lc, const Geom &g, Slots s, Inter in) {
     const int b = 256, n = (g.n_local + b - 1) / b;
-    StepParams p{};
-    k_firststep<false, true, false><<<n, b, 0, lc.stream>>>(g, s, in, p);
+    k_firststep<false, true, false><<<n, b, 0, lc.stream>>>(g, s, in, nullptr);
 }
 
-__global__ void k_inter_firststep(Inter in, StepParams p) {
+__global__ void k_inter_firststep(Inter in, const StepParams *__restrict__ p) {
     const int n = in.cnt[CNT_INTER];
+    const double dt = p->dt;
     for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
         const double c = dt_inv_m_of(p, in.type[a]);
         double vx = __dadd_rn(in.vx[a], __dmul_rn(c, in.fx[a]));
         double vy = __dadd_rn(in.vy[a], __dmul_rn(c, in.fy[a]));
         double vz = __dadd_rn(in.vz[a], __dmul_rn(c, in.fz[a]));
         in.vx[a] = vx; in.vy[a] = vy; in.vz[a] = vz;
-        in.x[a] = __dadd_rn(in.x[a], __dmul_rn(p.dt, vx));
-        in.y[a] = __dadd_rn(in.y[a], __dmul_rn(p.dt, vy));
-        in.z[a] = __dadd_rn(in.z[a], __dmul_rn(p.dt, vz));
+        in.x[a] = __dadd_rn(in.x[a], __dmul_rn(dt, vx));
+        in.y[a] = __dadd_rn(in.y[a], __dmul_rn(dt, vy));
+        in.z[a] = __dadd_rn(in.z[a], __dmul_rn(dt, vz));
     }
 }
-void launch_inter_firststep(const LaunchCtx &lc, Inter in, StepParams p) {
+void launch_inter_firststep(const LaunchCtx &lc, Inter in, const StepParams *p) {
     k_inter_firststep<<<lc.num_sms, 256, 0, lc.stream>>>(in, p);
 }
 
@@ -466,12 +456,12 @@ void launch_ghost_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool
 // atoms continue over the entries beyond the pruned set.
 // ------------------------------------------------------------------------------------------------
 template <int PAR>
-__device__ __forceinline__ double rho_sum_fp64(const Geom &g, const Slots &s, const PotTables &pt, int sl,
+__device__ __forceinline__ double rho_sum_fp64(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int sl,
                                                double xi, double yi, double zi, int q0, int q1) {
     double acc = 0.0;
 #pragma unroll 4
     for (int q = q0; q < q1; q++) {
-        const int sj = sl + c_lat[PAR][q];
+        const int sj = sl + nt.lat[PAR][q];
         const int tj = s.type[sj];
         if (tj < 0) continue;
         const double dx = xi - s.x[sj], dy = yi - s.y[sj], dz = zi - s.z[sj];
@@ -486,7 +476,7 @@ __device__ __forceinline__ double rho_sum_fp64(const Geom &g, const Slots &s, co
     return acc;
 }
 
-__global__ void __launch_bounds__(512) k_lat_rho_fp64(Geom g, Slots s, Inter in, PotTables pt, bool hook, int order) {
+__global__ void __launch_bounds__(512) k_lat_rho_fp64(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool hook, int order) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     int par;
     const int sl = gather_slot(g, t, order, par);
@@ -494,11 +484,11 @@ __global__ void __launch_bounds__(512) k_lat_rho_fp64(Geom g, Slots s, Inter in,
     const int ti = s.type[sl];
     if (ti < 0) { s.rho[sl] = 0.0; return; }
     const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
-    const int np = c_npruned;
-    double acc = par ? rho_sum_fp64<1>(g, s, pt, sl, xi, yi, zi, 0, np) : rho_sum_fp64<0>(g, s, pt, sl, xi, yi, zi, 0, np);
+    const int np = nt.npruned;
+    double acc = par ? rho_sum_fp64<1>(nt, g, s, pt, sl, xi, yi, zi, 0, np) : rho_sum_fp64<0>(nt, g, s, pt, sl, xi, yi, zi, 0, np);
     if (in.far_flag[sl]) {
-        const int nf = c_nfull;
-        acc += par ? rho_sum_fp64<1>(g, s, pt, sl, xi, yi, zi, np, nf) : rho_sum_fp64<0>(g, s, pt, sl, xi, yi, zi, np, nf);
+        const int nf = nt.nfull;
+        acc += par ? rho_sum_fp64<1>(nt, g, s, pt, sl, xi, yi, zi, np, nf) : rho_sum_fp64<0>(nt, g, s, pt, sl, xi, yi, zi, np, nf);
     }
     s.rho[sl] = acc;
     if (!hook && lattice_only(in)) {
@@ -509,16 +499,16 @@ __global__ void __launch_bounds__(512) k_lat_rho_fp64(Geom g, Slots s, Inter in,
 }
 
 template <int PAR>
-__device__ __forceinline__ void rho_sum_mixed(const Geom &g, const Slots &s, const PotTables &pt, int si, float4 ui,
+__device__ __forceinline__ void rho_sum_mixed(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int si, float4 ui,
                                               int q0, int q1, float &sum, float &comp) {
     const float rc2 = g.rc2_h;
     const float hinv = pt.h_inv_dr_f;
 #pragma unroll 4
     for (int q = q0; q < q1; q++) {
-        const float4 uj = __ldg(s.u4 + si + c_lats[PAR][q]);
+        const float4 uj = __ldg(s.u4 + si + nt.lats[PAR][q]);
         const int tj = __float_as_int(uj.w);
         if (tj < 0) continue;
-        const float4 D = c_dsite[PAR][q];
+        const float4 D = nt.dsite[PAR][q];
         const float dx = (ui.x - uj.x) - D.x, dy = (ui.y - uj.y) - D.y, dz = (ui.z - uj.z) - D.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (r2 < rc2) {
@@ -530,7 +520,7 @@ __device__ __forceinline__ void rho_sum_mixed(const Geom &g, const Slots &s, con
     }
 }
 
-__global__ void __launch_bounds__(512) k_lat_rho_mixed(Geom g, Slots s, Inter in, PotTables pt, bool hook, int order) {
+__global__ void __launch_bounds__(512) k_lat_rho_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool hook, int order) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     int par;
     const int sl = gather_slot(g, t, order, par);
@@ -540,13 +530,13 @@ __global__ void __launch_bounds__(512) k_lat_rho_mixed(Geom g, Slots s, Inter in
     const int ti = __float_as_int(ui.w);
     if (ti < 0) { s.rho[sl] = 0.0; return; }
     float sum = 0.f, comp = 0.f;
-    const int np = c_npruned;
-    if (par) rho_sum_mixed<1>(g, s, pt, si, ui, 0, np, sum, comp);
-    else rho_sum_mixed<0>(g, s, pt, si, ui, 0, np, sum, comp);
+    const int np = nt.npruned;
+    if (par) rho_sum_mixed<1>(nt, g, s, pt, si, ui, 0, np, sum, comp);
+    else rho_sum_mixed<0>(nt, g, s, pt, si, ui, 0, np, sum, comp);
     if (in.far_flag[sl]) {
-        const int nf = c_nfull;
-        if (par) rho_sum_mixed<1>(g, s, pt, si, ui, np, nf, sum, comp);
-        else rho_sum_mixed<0>(g, s, pt, si, ui, np, nf, sum, comp);
+        const int nf = nt.nfull;
+        if (par) rho_sum_mixed<1>(nt, g, s, pt, si, ui, np, nf, sum, comp);
+        else rho_sum_mixed<0>(nt, g, s, pt, si, ui, np, nf, sum, comp);
     }
     const double rho = (double) sum - (double) comp;
     s.rho[sl] = rho;
@@ -559,8 +549,8 @@ __global__ void __launch_bounds__(512) k_lat_rho_mixed(Geom g, Slots s, Inter in
 
 void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook) {
     const int order = lc.rho_order, b = lc.rho_block, n = (gather_threads(g, order) + b - 1) / b;
-    if (mixed) k_lat_rho_mixed<<<n, b, 0, lc.stream>>>(g, s, in, t, hook, order);
-    else k_lat_rho_fp64<<<n, b, 0, lc.stream>>>(g, s, in, t, hook, order);
+    if (mixed) k_lat_rho_mixed<<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order);
+    else k_lat_rho_fp64<<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order);
 }
 
 // dF/drho when inter atoms added density after the lattice pass (or for the df hook)
@@ -597,13 +587,13 @@ void launch_lat_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTab
 // phi = (r phi) / r.
 // ------------------------------------------------------------------------------------------------
 template <int PAR>
-__device__ __forceinline__ void force_sum_fp64(const Geom &g, const Slots &s, const PotTables &pt, int sl, int ti,
+__device__ __forceinline__ void force_sum_fp64(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int sl, int ti,
                                                double xi, double yi, double zi, double dfi, int q0, int q1,
                                                double &fx, double &fy, double &fz) {
     const Knot64 *rho_di = pt.rho_d + ti * pt.nr;
 #pragma unroll 2
     for (int q = q0; q < q1; q++) {
-        const int sj = sl + c_lat[PAR][q];
+        const int sj = sl + nt.lat[PAR][q];
         const int tj = s.type[sj];
         if (tj < 0) continue;
         const double dx = xi - s.x[sj], dy = yi - s.y[sj], dz = zi - s.z[sj];
@@ -629,7 +619,7 @@ __device__ __forceinline__ void force_sum_fp64(const Geom &g, const Slots &s, co
     }
 }
 
-__global__ void __launch_bounds__(512) k_lat_force_fp64(Geom g, Slots s, Inter in, PotTables pt, StepParams sp,
+__global__ void __launch_bounds__(512) k_lat_force_fp64(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, StepParams *sp,
                                                         bool kick, bool hook, int order) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     int par;
@@ -640,25 +630,27 @@ __global__ void __launch_bounds__(512) k_lat_force_fp64(Geom g, Slots s, Inter i
     const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
     const double dfi = s.df[sl];
     double fx = 0.0, fy = 0.0, fz = 0.0;
-    const int np = c_npruned;
-    if (par) force_sum_fp64<1>(g, s, pt, sl, ti, xi, yi, zi, dfi, 0, np, fx, fy, fz);
-    else force_sum_fp64<0>(g, s, pt, sl, ti, xi, yi, zi, dfi, 0, np, fx, fy, fz);
+    const int np = nt.npruned;
+    if (par) force_sum_fp64<1>(nt, g, s, pt, sl, ti, xi, yi, zi, dfi, 0, np, fx, fy, fz);
+    else force_sum_fp64<0>(nt, g, s, pt, sl, ti, xi, yi, zi, dfi, 0, np, fx, fy, fz);
     if (in.far_flag[sl]) {
-        const int nf = c_nfull;
-        if (par) force_sum_fp64<1>(g, s, pt, sl, ti, xi, yi, zi, dfi, np, nf, fx, fy, fz);
-        else force_sum_fp64<0>(g, s, pt, sl, ti, xi, yi, zi, dfi, np, nf, fx, fy, fz);
+        const int nf = nt.nfull;
+        if (par) force_sum_fp64<1>(nt, g, s, pt, sl, ti, xi, yi, zi, dfi, np, nf, fx, fy, fz);
+        else force_sum_fp64<0>(nt, g, s, pt, sl, ti, xi, yi, zi, dfi, np, nf, fx, fy, fz);
     }
     s.fx[sl] = fx; s.fy[sl] = fy; s.fz[sl] = fz;
     if (kick && !hook && lattice_only(in)) {
         const double c = dt_inv_m_of(sp, ti);
-        s.vx[sl] = __dadd_rn(s.vx[sl], __dmul_rn(c, fx));
-        s.vy[sl] = __dadd_rn(s.vy[sl], __dmul_rn(c, fy));
-        s.vz[sl] = __dadd_rn(s.vz[sl], __dmul_rn(c, fz));
+        const double vx = __dadd_rn(s.vx[sl], __dmul_rn(c, fx));
+        const double vy = __dadd_rn(s.vy[sl], __dmul_rn(c, fy));
+        const double vz = __dadd_rn(s.vz[sl], __dmul_rn(c, fz));
+        s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz;
+        note_vmax2(sp, speed2(vx, vy, vz));
     }
 }
 
 template <int PAR>
-__device__ __forceinline__ void force_sum_mixed(const Geom &g, const Slots &s, const PotTables &pt, int si, int ti,
+__device__ __forceinline__ void force_sum_mixed(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int si, int ti,
                                                 float4 ui, float dfi, int q0, int q1, float acc[6]) {
     const float rc2 = g.rc2_h;
     const float hinv = pt.h_inv_dr_f;
@@ -666,11 +658,11 @@ __device__ __forceinline__ void force_sum_mixed(const Geom &g, const Slots &s, c
     const float4 *rho_di = pt.rho_dff + ti * pt.nr;
 #pragma unroll 2
     for (int q = q0; q < q1; q++) {
-        const int oj = si + c_lats[PAR][q];
+        const int oj = si + nt.lats[PAR][q];
         const float4 uj = __ldg(s.u4 + oj);
         const int tj = __float_as_int(uj.w);
         if (tj < 0) continue;
-        const float4 D = c_dsite[PAR][q];
+        const float4 D = nt.dsite[PAR][q];
         const float dx = (ui.x - uj.x) - D.x, dy = (ui.y - uj.y) - D.y, dz = (ui.z - uj.z) - D.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (r2 < rc2) {
@@ -695,7 +687,7 @@ __device__ __forceinline__ void force_sum_mixed(const Geom &g, const Slots &s, c
     }
 }
 
-__global__ void __launch_bounds__(512) k_lat_force_mixed(Geom g, Slots s, Inter in, PotTables pt, StepParams sp,
+__global__ void __launch_bounds__(512) k_lat_force_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, StepParams *sp,
                                                          bool kick, bool hook, int order) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     int par;
@@ -707,13 +699,13 @@ __global__ void __launch_bounds__(512) k_lat_force_mixed(Geom g, Slots s, Inter 
     if (ti < 0) { s.fx[sl] = 0.0; s.fy[sl] = 0.0; s.fz[sl] = 0.0; return; }
     const float dfi = s.df32[si];
     float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // sums x, y, z and their Kahan compensations
-    const int np = c_npruned;
-    if (par) force_sum_mixed<1>(g, s, pt, si, ti, ui, dfi, 0, np, acc);
-    else force_sum_mixed<0>(g, s, pt, si, ti, ui, dfi, 0, np, acc);
+    const int np = nt.npruned;
+    if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, 0, np, acc);
+    else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, 0, np, acc);
     if (in.far_flag[sl]) {
-        const int nf = c_nfull;
-        if (par) force_sum_mixed<1>(g, s, pt, si, ti, ui, dfi, np, nf, acc);
-        else force_sum_mixed<0>(g, s, pt, si, ti, ui, dfi, np, nf, acc);
+        const int nf = nt.nfull;
+        if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, np, nf, acc);
+        else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, np, nf, acc);
     }
     const double h = 0.5 * g.a0;
     const double fx = h * ((double) acc[0] - (double) acc[3]);
@@ -722,26 +714,29 @@ __global__ void __launch_bounds__(512) k_lat_force_mixed(Geom g, Slots s, Inter 
     s.fx[sl] = fx; s.fy[sl] = fy; s.fz[sl] = fz;
     if (kick && !hook && lattice_only(in)) {
         const double c = dt_inv_m_of(sp, ti);
-        s.vx[sl] = __dadd_rn(s.vx[sl], __dmul_rn(c, fx));
-        s.vy[sl] = __dadd_rn(s.vy[sl], __dmul_rn(c, fy));
-        s.vz[sl] = __dadd_rn(s.vz[sl], __dmul_rn(c, fz));
+        const double vx = __dadd_rn(s.vx[sl], __dmul_rn(c, fx));
+        const double vy = __dadd_rn(s.vy[sl], __dmul_rn(c, fy));
+        const double vz = __dadd_rn(s.vz[sl], __dmul_rn(c, fz));
+        s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz;
+        note_vmax2(sp, speed2(vx, vy, vz));
     }
 }
 
-void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams p, bool kick,
+void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *p, bool kick,
                       bool mixed, bool hook) {
     const int order = lc.force_order, b = lc.force_block, n = (gather_threads(g, order) + b - 1) / b;
-    if (mixed) k_lat_force_mixed<<<n, b, 0, lc.stream>>>(g, s, in, t, p, kick, hook, order);
-    else k_lat_force_fp64<<<n, b, 0, lc.stream>>>(g, s, in, t, p, kick, hook, order);
+    if (mixed) k_lat_force_mixed<<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order);
+    else k_lat_force_fp64<<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order);
 }
 
 // second half-kick for lattice slots (only when inter atoms prevented fusion, or always) and for
 // inter atoms (src/newton_motion.cpp:57-74)
-__global__ void k_secondstep(Geom g, Slots s, Inter in, StepParams p, int lattice_mode) {
+__global__ void k_secondstep(Geom g, Slots s, Inter in, StepParams *p, int lattice_mode) {
     const int n_inter = in.cnt[CNT_INTER];
     const bool lattice = lattice_mode == 1 || (lattice_mode == 2 && !lattice_only(in));
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    double v2max = 0.0;
     if (lattice) {
         for (int t = t0; t < g.n_local; t += stride) {
             int i, j, k;
@@ -749,32 +744,103 @@ __global__ void k_secondstep(Geom g, Slots s, Inter in, StepParams p, int lattic
             const int ty = s.type[sl];
             if (ty < 0) continue;
             const double c = dt_inv_m_of(p, ty);
-            s.vx[sl] = __dadd_rn(s.vx[sl], __dmul_rn(c, s.fx[sl]));
-            s.vy[sl] = __dadd_rn(s.vy[sl], __dmul_rn(c, s.fy[sl]));
-            s.vz[sl] = __dadd_rn(s.vz[sl], __dmul_rn(c, s.fz[sl]));
+            const double vx = __dadd_rn(s.vx[sl], __dmul_rn(c, s.fx[sl]));
+            const double vy = __dadd_rn(s.vy[sl], __dmul_rn(c, s.fy[sl]));
+            const double vz = __dadd_rn(s.vz[sl], __dmul_rn(c, s.fz[sl]));
+            s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz;
+            v2max = fmax(v2max, speed2(vx, vy, vz));
         }
     }
     for (int a = t0; a < n_inter; a += stride) {
         const double c = dt_inv_m_of(p, in.type[a]);
-        in.vx[a] = __dadd_rn(in.vx[a], __dmul_rn(c, in.fx[a]));
-        in.vy[a] = __dadd_rn(in.vy[a], __dmul_rn(c, in.fy[a]));
-        in.vz[a] = __dadd_rn(in.vz[a], __dmul_rn(c, in.fz[a]));
+        const double vx = __dadd_rn(in.vx[a], __dmul_rn(c, in.fx[a]));
+        const double vy = __dadd_rn(in.vy[a], __dmul_rn(c, in.fy[a]));
+        const double vz = __dadd_rn(in.vz[a], __dmul_rn(c, in.fz[a]));
+        in.vx[a] = vx; in.vy[a] = vy; in.vz[a] = vz;
+        v2max = fmax(v2max, speed2(vx, vy, vz));
     }
+    if (v2max > 0.0) note_vmax2(p, v2max);
 }
-void launch_secondstep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams p, bool lattice) {
+void launch_secondstep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams *p, bool lattice) {
     k_secondstep<<<lc.num_sms * 8, 256, 0, lc.stream>>>(g, s, in, p, lattice ? 1 : 2);
+}
+
+// ------------------------------------------------------------------------------------------------
+// timestep control (extension: the reference sets dt per stage, src/newton_motion.cpp:13-28)
+// ------------------------------------------------------------------------------------------------
+// dt/(2m) per type as NewtonMotion::preComputeDtInv2m computes it: (0.5 * dt * ftm2v) / m
+__device__ __forceinline__ void set_dt_dev(StepParams *p, double dt) {
+    p->dt = dt;
+    const double dt_halve = __dmul_rn(__dmul_rn(0.5, dt), kFtm2v);
+    for (int t = 0; t < 3; t++) p->dt_inv_m[t] = __ddiv_rn(dt_halve, c_mass[t]);
+}
+__global__ void k_set_step(StepParams *p, double dt, double dx_max, double dt_min, double dt_max) {
+    p->dx_max = dx_max;
+    p->dt_min = dt_min;
+    p->dt_max = dt_max;
+    set_dt_dev(p, dt);
+}
+void launch_set_step(const LaunchCtx &lc, StepParams *sp, double dt, double dx_max, double dt_min, double dt_max) {
+    k_set_step<<<1, 1, 0, lc.stream>>>(sp, dt, dx_max, dt_min, dt_max);
+}
+// One block of kVmaxSlots threads: reduce and clear the max words, then (variable mode)
+// dt = clamp(dx_max / sqrt(max |v|^2), dt_min, dt_max); record dt and advance the clock.
+__global__ void __launch_bounds__(kVmaxSlots) k_step_head(StepParams *p) {
+    __shared__ unsigned long long part[kVmaxSlots / 32];
+    const unsigned long long b = p->vmax2[threadIdx.x];
+    p->vmax2[threadIdx.x] = 0ull;
+    const unsigned hi = (unsigned) (b >> 32), lo = (unsigned) b;
+    const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
+    const unsigned mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = ((unsigned long long) mhi << 32) | mlo;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    unsigned long long m = 0ull;
+    for (int w = 0; w < kVmaxSlots / 32; w++) m = part[w] > m ? part[w] : m;
+    if (p->dx_max > 0.0) {
+        const double v2 = __longlong_as_double((long long) m);
+        double dt = v2 > 0.0 ? __ddiv_rn(p->dx_max, __dsqrt_rn(v2)) : p->dt_max;
+        if (dt < p->dt_min) dt = p->dt_min;
+        if (dt > p->dt_max) dt = p->dt_max;
+        set_dt_dev(p, dt);
+    }
+    const long long k = p->steps;
+    p->hist[k % kDtHistory] = p->dt;
+    p->time = __dadd_rn(p->time, p->dt);
+    p->steps = k + 1;
+}
+void launch_step_head(const LaunchCtx &lc, StepParams *sp) { k_step_head<<<1, kVmaxSlots, 0, lc.stream>>>(sp); }
+// max |v|^2 over local lattice atoms and local inter atoms, from scratch
+__global__ void k_vmax_full(Geom g, Slots s, Inter in, StepParams *p) {
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    double v2max = 0.0;
+    for (int t = t0; t < g.n_local; t += stride) {
+        int i, j, k;
+        const int sl = local_slot(g, t, i, j, k);
+        if (s.type[sl] < 0) continue;
+        v2max = fmax(v2max, speed2(s.vx[sl], s.vy[sl], s.vz[sl]));
+    }
+    const int n_inter = in.cnt[CNT_INTER];
+    for (int a = t0; a < n_inter; a += stride) v2max = fmax(v2max, speed2(in.vx[a], in.vy[a], in.vz[a]));
+    if (v2max > 0.0) note_vmax2(p, v2max);
+}
+void launch_vmax_full(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams *sp) {
+    cudaMemsetAsync(reinterpret_cast<char *>(sp) + offsetof(StepParams, vmax2), 0, sizeof(unsigned long long) * kVmaxSlots,
+                    lc.stream);
+    k_vmax_full<<<lc.num_sms * 8, 256, 0, lc.stream>>>(g, s, in, sp);
 }
 
 // ------------------------------------------------------------------------------------------------
 // per-atom energy (extension): e_i = F(rho_i) + 1/2 sum_j phi_ij over lattice neighbours
 // ------------------------------------------------------------------------------------------------
 template <int PAR>
-__device__ __forceinline__ double energy_sum_fp64(const Geom &g, const Slots &s, const PotTables &pt, int sl, int ti,
+__device__ __forceinline__ double energy_sum_fp64(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int sl, int ti,
                                                   int q0, int q1) {
     const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
     double acc = 0.0;
     for (int q = q0; q < q1; q++) {
-        const int sj = sl + c_lat[PAR][q];
+        const int sj = sl + nt.lat[PAR][q];
         const int tj = s.type[sj];
         if (tj < 0) continue;
         const double dx = xi - s.x[sj], dy = yi - s.y[sj], dz = zi - s.z[sj];
@@ -789,14 +855,14 @@ __device__ __forceinline__ double energy_sum_fp64(const Geom &g, const Slots &s,
     return acc;
 }
 template <int PAR>
-__device__ __forceinline__ void energy_sum_mixed(const Geom &g, const Slots &s, const PotTables &pt, int si, int ti,
+__device__ __forceinline__ void energy_sum_mixed(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int si, int ti,
                                                  float4 ui, int q0, int q1, float &sum, float &comp) {
     const float inv_h = 1.0f / g.h_f;
     for (int q = q0; q < q1; q++) {
-        const float4 uj = __ldg(s.u4 + si + c_lats[PAR][q]);
+        const float4 uj = __ldg(s.u4 + si + nt.lats[PAR][q]);
         const int tj = __float_as_int(uj.w);
         if (tj < 0) continue;
-        const float4 D = c_dsite[PAR][q];
+        const float4 D = nt.dsite[PAR][q];
         const float dx = (ui.x - uj.x) - D.x, dy = (ui.y - uj.y) - D.y, dz = (ui.z - uj.z) - D.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (r2 < g.rc2_h) {
@@ -809,18 +875,18 @@ __device__ __forceinline__ void energy_sum_mixed(const Geom &g, const Slots &s, 
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(256) k_energy(Geom g, Slots s, Inter in, PotTables pt, int order) {
+__global__ void __launch_bounds__(256) k_energy(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, int order) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     int par;
     const int sl = gather_slot(g, t, order, par);
     if (sl < 0) return;
     const int ti = s.type[sl];
     if (ti < 0) { s.e[sl] = 0.0; return; }
-    const int np = c_npruned;
-    const int nq = in.far_flag[sl] ? c_nfull : np;
+    const int np = nt.npruned;
+    const int nq = in.far_flag[sl] ? nt.nfull : np;
     if (!MIXED) {
-        double acc = par ? energy_sum_fp64<1>(g, s, pt, sl, ti, 0, np) : energy_sum_fp64<0>(g, s, pt, sl, ti, 0, np);
-        if (nq > np) acc += par ? energy_sum_fp64<1>(g, s, pt, sl, ti, np, nq) : energy_sum_fp64<0>(g, s, pt, sl, ti, np, nq);
+        double acc = par ? energy_sum_fp64<1>(nt, g, s, pt, sl, ti, 0, np) : energy_sum_fp64<0>(nt, g, s, pt, sl, ti, 0, np);
+        if (nq > np) acc += par ? energy_sum_fp64<1>(nt, g, s, pt, sl, ti, np, nq) : energy_sum_fp64<0>(nt, g, s, pt, sl, ti, np, nq);
         int m; double p;
         locate_d(s.rho[sl], pt.inv_drho, pt.nrho, m, p);
         s.e[sl] = val_d(pt.F_v + ti * pt.nrho, m, p) + 0.5 * acc;
@@ -828,11 +894,11 @@ __global__ void __launch_bounds__(256) k_energy(Geom g, Slots s, Inter in, PotTa
         const int si = sidx(g, sl);
         const float4 ui = s.u4[si];
         float sum = 0.f, comp = 0.f;
-        if (par) energy_sum_mixed<1>(g, s, pt, si, ti, ui, 0, np, sum, comp);
-        else energy_sum_mixed<0>(g, s, pt, si, ti, ui, 0, np, sum, comp);
+        if (par) energy_sum_mixed<1>(nt, g, s, pt, si, ti, ui, 0, np, sum, comp);
+        else energy_sum_mixed<0>(nt, g, s, pt, si, ti, ui, 0, np, sum, comp);
         if (nq > np) {
-            if (par) energy_sum_mixed<1>(g, s, pt, si, ti, ui, np, nq, sum, comp);
-            else energy_sum_mixed<0>(g, s, pt, si, ti, ui, np, nq, sum, comp);
+            if (par) energy_sum_mixed<1>(nt, g, s, pt, si, ti, ui, np, nq, sum, comp);
+            else energy_sum_mixed<0>(nt, g, s, pt, si, ti, ui, np, nq, sum, comp);
         }
         int m; float p;
         locate_f((float) s.rho[sl], pt.inv_drho_f, pt.nrho, m, p);
@@ -841,8 +907,8 @@ __global__ void __launch_bounds__(256) k_energy(Geom g, Slots s, Inter in, PotTa
 }
 void launch_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
     const int b = 256, n = (gather_threads(g, 0) + b - 1) / b;
-    if (mixed) k_energy<true><<<n, b, 0, lc.stream>>>(g, s, in, t, 0);
-    else k_energy<false><<<n, b, 0, lc.stream>>>(g, s, in, t, 0);
+    if (mixed) k_energy<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, 0);
+    else k_energy<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, 0);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -853,14 +919,15 @@ void launch_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTab
 // owner of a ghost slot in i's neighbourhood, so it is marked too.) Clearing writes 0 over the same
 // slots of the old list. Work item e of a flat loop covers (far atom e / (nfull + 1), entry).
 // ------------------------------------------------------------------------------------------------
-__device__ void mark_far_neighbourhoods(const Geom &g, const Inter &in, int a0, int a1, int8_t v, int t0, int nt) {
-    const int per = c_nfull + 1;
+__device__ void mark_far_neighbourhoods(const NeighTables &nt, const Geom &g, const Inter &in, int a0, int a1, int8_t v, int t0,
+                                        int stride) {
+    const int per = nt.nfull + 1;
     const int total = (a1 - a0) * per;
-    for (int e = t0; e < total; e += nt) {
+    for (int e = t0; e < total; e += stride) {
         const int sl = in.far_list[a0 + e / per];
         const int q = e % per;
         const int par = (sl % g.Sx) & 1;
-        const int sj = q == c_nfull ? sl : sl + (par ? c_lat[1][q] : c_lat[0][q]);
+        const int sj = q == nt.nfull ? sl : sl + (par ? nt.lat[1][q] : nt.lat[0][q]);
         in.far_flag[owner_slot(g, sj)] = v;
     }
 }
@@ -948,9 +1015,9 @@ __device__ __forceinline__ void region_fw(const Geom &g, int d, int dir, int lo[
     else { lo[d] = bb[d]; hi[d] = bb[d] + gg[d]; }
 }
 
-__global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s, Inter in, int mask, bool mixed) {
+__global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, int mask, bool mixed) {
     __shared__ int sh_n;
-    const int tid = threadIdx.x, nt = blockDim.x;
+    const int tid = threadIdx.x, nthr = blockDim.x;
 
     if (mask & MANAGE_CLEAR_GHOST) {
         if (tid == 0) in.cnt[CNT_GHOST] = 0;
@@ -961,7 +1028,7 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s
         // the far list of the previous step is void: every lattice atom is re-tested below
         {
             const int nf = min(in.cnt[CNT_FAR], in.fcap);
-            mark_far_neighbourhoods(g, in, 0, nf, 0, tid, nt);
+            mark_far_neighbourhoods(nt, g, in, 0, nf, 0, tid, nthr);
             __syncthreads();
             if (tid == 0) in.cnt[CNT_FAR] = 0;
             __syncthreads();
@@ -972,12 +1039,12 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s
         const int n0 = in.cnt[CNT_INTER];
         if (nd > 0) {
             long long *keys = in.bucket;  // reused as sort buffer
-            for (int q = tid; q < nd; q += nt) keys[q] = in.displaced[q];
+            for (int q = tid; q < nd; q += nthr) keys[q] = in.displaced[q];
             __syncthreads();
             block_bitonic_sort(keys, nd);
             int room = in.cap - n0;
             if (nd > room) { if (tid == 0) set_error(in, MG_DEVERR_INTER_OVERFLOW); nd = room; }
-            for (int q = tid; q < nd; q += nt) {
+            for (int q = tid; q < nd; q += nthr) {
                 const int sl = (int) keys[q];
                 const int a = n0 + q;
                 in.id[a] = s.id[sl];
@@ -1000,7 +1067,7 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s
         // (ii) recombination with vacancies, first claimant in list order wins
         const int n = in.cnt[CNT_INTER];
         int *cand = in.scratch_i + in.cap;  // n ints
-        for (int a = tid; a < n; a += nt) {
+        for (int a = tid; a < n; a += nthr) {
             const int near = near_index_in_sub_box(g, in.x[a], in.y[a], in.z[a]);
             int c = -1;
             if (near >= 0 && s.type[near] == kInvalid && is_out_box(g, s.x[near], s.y[near], s.z[near]) == kInBox) {
@@ -1011,10 +1078,10 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s
         }
         __syncthreads();
         int *won = in.scratch_i + in.cap + in.cap;  // n ints
-        for (int a = tid; a < n; a += nt) won[a] = (cand[a] >= 0 && in.claim[cand[a]] == a) ? 1 : 0;
+        for (int a = tid; a < n; a += nthr) won[a] = (cand[a] >= 0 && in.claim[cand[a]] == a) ? 1 : 0;
         __syncthreads();
-        for (int a = tid; a < n; a += nt) if (cand[a] >= 0) in.claim[cand[a]] = INT_MAX;
-        for (int a = tid; a < n; a += nt) {
+        for (int a = tid; a < n; a += nthr) if (cand[a] >= 0) in.claim[cand[a]] = INT_MAX;
+        for (int a = tid; a < n; a += nthr) {
             if (!won[a]) continue;
             const int sl = cand[a];
             s.id[sl] = in.id[a];
@@ -1035,11 +1102,11 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s
             }
         }
         __syncthreads();
-        mark_far_neighbourhoods(g, in, 0, min(in.cnt[CNT_FAR], in.fcap), 1, tid, nt);
+        mark_far_neighbourhoods(nt, g, in, 0, min(in.cnt[CNT_FAR], in.fcap), 1, tid, nthr);
         __syncthreads();
         // stable compaction of the survivors
         int base = 0;
-        for (int c0 = 0; c0 < n; c0 += nt) {
+        for (int c0 = 0; c0 < n; c0 += nthr) {
             const int a = c0 + tid;
             const int keep = (a < n && !won[a]) ? 1 : 0;
             int ex;
@@ -1048,7 +1115,7 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s
             base += tot;
         }
         __syncthreads();
-        for (int a = tid; a < base; a += nt) inter_restore(in, a, a);
+        for (int a = tid; a < base; a += nthr) inter_restore(in, a, a);
         if (tid == 0) in.cnt[CNT_INTER] = base;
         __syncthreads();
     }
@@ -1058,14 +1125,14 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s
         for (int d = 0; d < 3; d++) {
             const int n = in.cnt[CNT_INTER];
             int *cls = in.scratch_i + in.cap;  // 0 stay, 1 lower, 2 higher
-            for (int a = tid; a < n; a += nt) {
+            for (int a = tid; a < n; a += nthr) {
                 const uint32_t f = is_out_box(g, in.x[a], in.y[a], in.z[a]);
                 cls[a] = (f & lowf[d]) ? 1 : ((f & highf[d]) ? 2 : 0);
             }
             __syncthreads();
             int base = 0;
             for (int which = 0; which < 3; which++) {
-                for (int c0 = 0; c0 < n; c0 += nt) {
+                for (int c0 = 0; c0 < n; c0 += nthr) {
                     const int a = c0 + tid;
                     const int sel = (a < n && cls[a] == which) ? 1 : 0;
                     int ex;
@@ -1084,7 +1151,7 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s
                 }
             }
             __syncthreads();
-            for (int a = tid; a < n; a += nt) inter_restore(in, a, a);
+            for (int a = tid; a < n; a += nthr) inter_restore(in, a, a);
             __syncthreads();
         }
     }
@@ -1102,7 +1169,7 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s
                 __syncthreads();
                 const int base0 = sh_n;
                 int base = base0;
-                for (int c0 = 0; c0 < total; c0 += nt) {
+                for (int c0 = 0; c0 < total; c0 += nthr) {
                     const int e = c0 + tid;
                     int sel = 0;
                     double px = 0, py = 0, pz = 0;
@@ -1146,7 +1213,7 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s
         const int n_loc = in.cnt[CNT_INTER];
         const int n_gh = in.cnt[CNT_GHOST];
         const int total = n_loc + n_gh;
-        for (int e = tid; e < total; e += nt) {
+        for (int e = tid; e < total; e += nthr) {
             double px, py, pz;
             int ref;
             if (e < n_loc) { px = in.x[e]; py = in.y[e]; pz = in.z[e]; ref = e; }
@@ -1169,7 +1236,7 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(Geom g, Slots s
 }
 
 void launch_inter_manage(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, int mask, bool mixed) {
-    k_inter_manage<<<1, kManageThreads, 0, lc.stream>>>(g, s, in, mask, mixed);
+    k_inter_manage<<<1, kManageThreads, 0, lc.stream>>>(*lc.nt, g, s, in, mask, mixed);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -1230,7 +1297,7 @@ __device__ __forceinline__ double lat_df(const Geom &g, const Slots &s, int sl, 
 
 // kind: 0 density, 1 force, 2 energy
 template <int KIND>
-__global__ void k_inter_eam(Geom g, Slots s, Inter in, PotTables pt, bool mixed) {
+__global__ void k_inter_eam(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool mixed) {
     const int n = in.cnt[CNT_INTER];
     const int nb = *in.n_bucket;
     for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
@@ -1243,9 +1310,9 @@ __global__ void k_inter_eam(Geom g, Slots s, Inter in, PotTables pt, bool mixed)
         double acc = 0.0, fx = 0.0, fy = 0.0, fz = 0.0;
         // lattice partners: the nearest site's atom, then the full offsets of that site
         const int par = (near % g.Sx) & 1;
-        const int nf = c_nfull;
+        const int nf = nt.nfull;
         for (int q = -1; q < nf; q++) {
-            const int sj = q < 0 ? near : near + (par ? c_full[1][q] : c_full[0][q]);
+            const int sj = q < 0 ? near : near + (par ? nt.full[1][q] : nt.full[0][q]);
             if (sj < 0 || sj >= g.n_slots) { set_error(in, MG_DEVERR_OUT_OF_GRID); continue; }
             const int tj = s.type[sj];
             if (tj < 0) continue;
@@ -1270,7 +1337,7 @@ __global__ void k_inter_eam(Geom g, Slots s, Inter in, PotTables pt, bool mixed)
         }
         // inter partners: same-site bucket (not itself), then the buckets of the full offsets
         for (int q = -1; q < nf; q++) {
-            const int key = q < 0 ? near : near + (par ? c_full[1][q] : c_full[0][q]);
+            const int key = q < 0 ? near : near + (par ? nt.full[1][q] : nt.full[0][q]);
             for (int b = bucket_begin(in, nb, key); b < nb && (int) (in.bucket[b] >> 32) == key; b++) {
                 const InterRef o = inter_ref(in, (int) (in.bucket[b] & 0xffffffffLL));
                 if (q < 0 && o.id == ida) continue;
@@ -1301,22 +1368,22 @@ __global__ void k_inter_eam(Geom g, Slots s, Inter in, PotTables pt, bool mixed)
     }
 }
 void launch_inter_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
-    k_inter_eam<0><<<lc.num_sms, 128, 0, lc.stream>>>(g, s, in, t, mixed);
+    k_inter_eam<0><<<lc.num_sms, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
 }
 void launch_inter_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
-    k_inter_eam<1><<<lc.num_sms, 128, 0, lc.stream>>>(g, s, in, t, mixed);
+    k_inter_eam<1><<<lc.num_sms, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
 }
 void launch_inter_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
-    k_inter_eam<2><<<lc.num_sms, 128, 0, lc.stream>>>(g, s, in, t, mixed);
+    k_inter_eam<2><<<lc.num_sms, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
 }
 
 // ------------------------------------------------------------------------------------------------
 // far lattice atoms (farther than 0.2 a0 from their site). Rebuild from positions for states that did
 // not come through atom::decide (uploads, the per-phase hooks).
 // ------------------------------------------------------------------------------------------------
-__global__ void k_far_clear(Geom g, Inter in) {
+__global__ void k_far_clear(const __grid_constant__ NeighTables nt, Geom g, Inter in) {
     const int nf = min(in.cnt[CNT_FAR], in.fcap);
-    mark_far_neighbourhoods(g, in, 0, nf, 0, threadIdx.x, blockDim.x);
+    mark_far_neighbourhoods(nt, g, in, 0, nf, 0, threadIdx.x, blockDim.x);
     __syncthreads();
     if (threadIdx.x == 0) in.cnt[CNT_FAR] = 0;
 }
@@ -1332,15 +1399,15 @@ __global__ void k_far_scan(Geom g, Slots s, Inter in) {
         else set_error(in, MG_DEVERR_DISPLACED_OVERFLOW);
     }
 }
-__global__ void k_far_mark(Geom g, Inter in) {
+__global__ void k_far_mark(const __grid_constant__ NeighTables nt, Geom g, Inter in) {
     const int nf = min(in.cnt[CNT_FAR], in.fcap);
-    mark_far_neighbourhoods(g, in, 0, nf, 1, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+    mark_far_neighbourhoods(nt, g, in, 0, nf, 1, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 void launch_far_rebuild(const LaunchCtx &lc, const Geom &g, Slots s, Inter in) {
-    k_far_clear<<<1, 1024, 0, lc.stream>>>(g, in);
+    k_far_clear<<<1, 1024, 0, lc.stream>>>(*lc.nt, g, in);
     const int b = 256;
     k_far_scan<<<(g.n_local + b - 1) / b, b, 0, lc.stream>>>(g, s, in);
-    k_far_mark<<<lc.num_sms, 256, 0, lc.stream>>>(g, in);
+    k_far_mark<<<lc.num_sms, 256, 0, lc.stream>>>(*lc.nt, g, in);
 }
 
 

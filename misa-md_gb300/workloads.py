@@ -62,6 +62,9 @@ class PotentialSpec:
     r_on: float = 5.0
     rho_max: float = 200.0
     lattice_const: float = 2.855
+    core: bool = True       # screened-Coulomb core below core_r2, joined to the Morse term on [core_r1, core_r2]
+    core_r1: float = 1.0
+    core_r2: float = 2.0
     params: list = field(default_factory=list)
 
     def __post_init__(self):
@@ -83,6 +86,25 @@ def _switch(r, r_on, rc):
     return 1.0 - 10.0 * t**3 + 15.0 * t**4 - 6.0 * t**5
 
 
+# Universal screening function of Ziegler, Biersack and Littmark (The Stopping and Range of Ions in
+# Solids, 1985): phi(r) = Zi Zj e^2 / (4 pi eps0 r) * sum_k c_k exp(-d_k r / a),
+# a = 0.8854 a_Bohr / (Zi^0.23 + Zj^0.23).
+ZBL_C = (0.18175, 0.50986, 0.28022, 0.02817)
+ZBL_D = (3.19980, 0.94229, 0.40290, 0.20162)
+COULOMB_EV_A = 14.399645   # e^2 / (4 pi eps0) in eV * Angstrom
+
+
+def zbl_rphi(r, zi, zj):
+    """r * phi_ZBL(r) in eV * Angstrom (finite at r = 0)."""
+    a = 0.46850 / (zi ** 0.23 + zj ** 0.23)
+    return COULOMB_EV_A * zi * zj * sum(c * np.exp(-d * r / a) for c, d in zip(ZBL_C, ZBL_D))
+
+
+def _smoothstep(r, r1, r2):
+    t = np.clip((r - r1) / (r2 - r1), 0.0, 1.0)
+    return 10.0 * t**3 - 15.0 * t**4 + 6.0 * t**5
+
+
 def potential_tables(spec: PotentialSpec):
     """Return (F[e][nrho], rho[e][nr], rphi[pair][nr], drho, dr) for the setfl body."""
     dr = spec.cutoff / (spec.nr - 1)
@@ -100,14 +122,21 @@ def potential_tables(spec: PotentialSpec):
             a = math.sqrt(pi.alpha * pj.alpha)
             r0 = math.sqrt(pi.r0 * pj.r0)
             phi = D * (np.exp(-2.0 * a * (r - r0)) - 2.0 * np.exp(-a * (r - r0))) * sw
-            pairs.append(r * phi)
+            rphi = r * phi
+            if spec.core:
+                # displacement cascades bring atoms to a fraction of an Angstrom: a Morse term alone
+                # peaks near 0.4 keV at r = 0 and lets keV recoils pass through atoms
+                s = _smoothstep(r, spec.core_r1, spec.core_r2)
+                rphi = (1.0 - s) * zbl_rphi(r, ATOMIC_NUMBER[i], ATOMIC_NUMBER[j]) + s * rphi
+            pairs.append(rphi)
     return F, rho, np.stack(pairs), drho, dr
 
 
 def write_setfl(path: str, spec: PotentialSpec) -> str:
     F, rho, rphi, drho, dr = potential_tables(spec)
     lines = [
-        "synthetic EAM: Morse pair, exponential density, -sqrt(rho) embedding",
+        "synthetic EAM: Morse pair, exponential density, -sqrt(rho) embedding" +
+        (f", ZBL core joined on [{spec.core_r1}, {spec.core_r2}] A" if spec.core else ""),
         f"seed {spec.seed}; quintic switch on [{spec.r_on}, {spec.cutoff}] A",
         "generated by misa-md_gb300/workloads.py",
         f"{spec.n_ele} " + " ".join(SYMBOL[:spec.n_ele]),
@@ -169,6 +198,7 @@ class Workload:
     dt: float = 0.001
     steps: int = 100
     seed: int = 1234
+    pka_ev: float = 0.0          # cascades: PKA energy at the central site, direction from the seed
 
     @property
     def cutoff_radius_factor(self) -> float:
@@ -179,14 +209,63 @@ class Workload:
         return 2 * self.cells[0] * self.cells[1] * self.cells[2]
 
 
-# The five workloads of the benchmark set (sizes, compositions, temperatures, steps).
+# Variable timestep of the cascade workloads: at most 0.01 A per step, 0.01 - 1 fs (Angstrom, ps).
+CASCADE_DX_MAX, CASCADE_DT_MIN, CASCADE_DT_MAX = 0.01, 1e-5, 1e-3
+
+# The single-box workloads of the benchmark set (sizes, compositions, temperatures, steps).
 WORKLOADS = {
     "fe_20c": Workload("fe_20c", (20, 20, 20), temperature=600.0, steps=100),
     "fe_100c": Workload("fe_100c", (100, 100, 100), temperature=600.0, steps=1000),
     "fecuni_200c": Workload("fecuni_200c", (200, 200, 200), n_ele=3, cu_frac=0.015, ni_frac=0.010,
                             temperature=600.0, steps=500),
-    "fe_100c_cascade": Workload("fe_100c_cascade", (100, 100, 100), temperature=300.0, steps=2000),
+    "fe_100c_cascade": Workload("fe_100c_cascade", (100, 100, 100), temperature=300.0, steps=2000,
+                                pka_ev=5000.0),
 }
+
+
+@dataclass
+class CascadeSet:
+    """Independent cascade replicas: cubic boxes with edges drawn uniformly from [cells_lo, cells_hi]
+    unit cells, the Fe-Cu-Ni composition, PKA energies uniform in [energy_lo, energy_hi] eV with
+    random directions, each replica on its own variable timestep."""
+    name: str = "fecuni_cascades_64"
+    replicas: int = 64
+    cells_lo: int = 40
+    cells_hi: int = 80
+    energy_lo: float = 1000.0
+    energy_hi: float = 10000.0
+    temperature: float = 300.0
+    steps: int = 1500
+    n_ele: int = 3
+    cu_frac: float = 0.015
+    ni_frac: float = 0.010
+    lattice_const: float = 2.855
+    cutoff: float = 5.6
+    seed: int = 4321
+
+    @property
+    def cutoff_radius_factor(self) -> float:
+        return self.cutoff / self.lattice_const
+
+    def replica_specs(self):
+        """Per replica: cells, PKA lattice site [x, y, z, basis], direction, energy (eV), state seed."""
+        rng = np.random.default_rng(self.seed)
+        out = []
+        for r in range(self.replicas):
+            n = int(rng.integers(self.cells_lo, self.cells_hi + 1))
+            e = float(rng.uniform(self.energy_lo, self.energy_hi))
+            d = rng.standard_normal(3)
+            out.append({"cells": (n, n, n), "lat": [n // 2, n // 2, n // 2, 0], "dir": d / np.linalg.norm(d),
+                        "energy": e, "seed": self.seed + 1 + r})
+        return out
+
+    def potential_workload(self) -> "Workload":
+        return Workload(self.name, (self.cells_lo,) * 3, lattice_const=self.lattice_const, cutoff=self.cutoff,
+                        n_ele=self.n_ele, cu_frac=self.cu_frac, ni_frac=self.ni_frac,
+                        temperature=self.temperature, seed=1234)
+
+
+CASCADE_SETS = {"fecuni_cascades_64": CascadeSet()}
 
 
 def build_state(cells, lattice_const, cutoff_radius_factor, *, temperature=600.0, seed=1234,

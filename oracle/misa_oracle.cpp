@@ -384,6 +384,10 @@ struct orc_sim {
     double rc = 0;
     double dt = 0;
     double dt_inv_m[3] = {0, 0, 0};
+    // variable timestep (extension, not in the reference): dx_max <= 0 keeps dt fixed
+    double dx_max = 0, dt_min = 0, dt_max = 0;
+    std::vector<double> dt_hist;  // dt of every step taken
+    double sim_time = 0;
 
     int64_t n_slots() const { return dom.dbx_ext[0] * dom.dbx_ext[1] * dom.dbx_ext[2]; }
     int64_t idx(int64_t x, int64_t y, int64_t z) const { return lin_index(dom, x, y, z); }
@@ -991,7 +995,32 @@ struct orc_sim {
         return total;
     }
 
+    // dt = clamp(dx_max / max|v|, dt_min, dt_max), max over local lattice and local inter atoms of
+    // (vx^2 + vy^2) + vz^2; every operation is a single IEEE rounding (built with -ffp-contract=off)
+    double max_speed2() {
+        double m = 0.0;
+        auto note = [&](const orc_atom &a) {
+            const double v2 = (a.v[0] * a.v[0] + a.v[1] * a.v[1]) + a.v[2] * a.v[2];
+            if (v2 > m) m = v2;
+        };
+        foreach_sub_box([&](orc_atom &a, int64_t, int64_t, int64_t) { if (a.type != kInvalid) note(a); });
+        for (const orc_atom &a : inter_list) note(a);
+        return m;
+    }
+    void step_head() {
+        if (dx_max > 0) {
+            const double v2 = max_speed2();
+            double t = v2 > 0.0 ? dx_max / std::sqrt(v2) : dt_max;
+            if (t < dt_min) t = dt_min;
+            if (t > dt_max) t = dt_max;
+            set_dt(t);
+        }
+        dt_hist.push_back(dt);
+        sim_time += dt;
+    }
+
     void step() {
+        step_head();
         firststep();
         decide();
         exchange_inter();
@@ -1097,7 +1126,20 @@ void orc_set_inter(orc_sim *s, const orc_atom *in, int64_t n) {
     s->inter_list.clear();
     for (int64_t i = 0; i < n; i++) s->inter_list.push_back(in[i]);
 }
-void orc_set_timestep(orc_sim *s, double dt) { s->set_dt(dt); }
+void orc_set_timestep(orc_sim *s, double dt) { s->set_dt(dt); s->dx_max = 0; }
+void orc_set_variable_timestep(orc_sim *s, double dx_max, double dt_min, double dt_max) {
+    s->dx_max = dx_max;
+    s->dt_min = dt_min;
+    s->dt_max = dt_max;
+    s->set_dt(dt_max);
+}
+double orc_max_speed2(orc_sim *s) { return s->max_speed2(); }
+int64_t orc_dt_history(const orc_sim *s, double *out, int64_t cap) {
+    const int64_t n = static_cast<int64_t>(s->dt_hist.size());
+    for (int64_t i = 0; i < n && i < cap; i++) out[i] = s->dt_hist[i];
+    return n;
+}
+double orc_time(const orc_sim *s) { return s->sim_time; }
 
 void orc_firststep(orc_sim *s) { s->firststep(); }
 int32_t orc_decide(orc_sim *s) { return s->decide(); }

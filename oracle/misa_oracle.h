@@ -82,6 +82,13 @@ int64_t orc_get_ghost_inter(const orc_sim *s, orc_atom *out, int64_t cap);
 void orc_set_inter(orc_sim *s, const orc_atom *in, int64_t n);
 
 void orc_set_timestep(orc_sim *s, double dt_ps);
+/* Variable timestep (extension, not in the reference): before each step of orc_simulate,
+ * dt = clamp(dx_max / max|v|, dt_min, dt_max) over local lattice and local inter atoms. */
+void orc_set_variable_timestep(orc_sim *s, double dx_max, double dt_min_ps, double dt_max_ps);
+double orc_max_speed2(orc_sim *s);
+/* dt of every step orc_simulate took (returns the count; copies at most cap), and their sum. */
+int64_t orc_dt_history(const orc_sim *s, double *out, int64_t cap);
+double orc_time(const orc_sim *s);
 
 /* Pieces of one step, in src/simulation.cpp:238-268 order. */
 void orc_firststep(orc_sim *s);

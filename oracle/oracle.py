@@ -57,6 +57,10 @@ _PROTOS = {
     "orc_get_ghost_inter": (_I64, [_P, _P, _I64]),
     "orc_set_inter": (None, [_P, _P, _I64]),
     "orc_set_timestep": (None, [_P, _D]),
+    "orc_set_variable_timestep": (None, [_P, _D, _D, _D]),
+    "orc_max_speed2": (_D, [_P]),
+    "orc_dt_history": (_I64, [_P, _P, _I64]),
+    "orc_time": (_D, [_P]),
     "orc_firststep": (None, [_P]),
     "orc_decide": (_I32, [_P]),
     "orc_exchange_inter": (None, [_P]),
@@ -221,6 +225,16 @@ class OracleSim:
 
     def set_timestep(self, dt):
         self.L.orc_set_timestep(self.h, float(dt))
+
+    def set_variable_timestep(self, dx_max, dt_min, dt_max):
+        self.L.orc_set_variable_timestep(self.h, float(dx_max), float(dt_min), float(dt_max))
+
+    def dt_history(self):
+        n = self.L.orc_dt_history(self.h, None, 0)
+        out = np.zeros(n)
+        if n:
+            self.L.orc_dt_history(self.h, _ptr(out), n)
+        return out
 
     def __getattr__(self, name):
         # thin pass-through for the step pieces: firststep, decide, exchange_inter, ...

@@ -411,3 +411,25 @@ def test_autotune_keeps_results_bit_identical(pkg, wl, potentials, gpu_lib, prec
         ctx.close()
     for r in runs[1:]:
         assert np.array_equal(r["x"], runs[0]["x"]) and np.array_equal(r["f"], runs[0]["f"])
+
+
+def test_contexts_with_different_boxes_coexist(pkg, orc, wl, potentials, gpu_lib):
+    """Each context carries its own offset tables: interleaved steps of two differently sized boxes
+    must each match their own oracle."""
+    pairs = []
+    for cells, seed in (((8, 8, 8), 91), ((11, 9, 10), 92)):
+        atoms = wl.build_state(cells, A0, RCF, temperature=600.0, seed=seed)
+        ctx, ref = make_pair(pkg, orc, wl, potentials["fe"], cells, atoms)
+        ctx.prepare()
+        ref.prepare()
+        pairs.append((cells, ctx, ref))
+    for _ in range(3):
+        for cells, ctx, ref in pairs:
+            ctx.simulate(2)
+            ref.simulate(2)
+    for cells, ctx, ref in pairs:
+        got, _ = ctx.download()
+        want = ref.get_atoms()
+        loc = local(wl, cells)
+        assert np.abs(got["f"][loc] - want["f"][loc]).max() < F64_TOL
+        ctx.close()
