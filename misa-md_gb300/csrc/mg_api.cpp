@@ -196,6 +196,12 @@ mg_status ensure_aos(mg_context *ctx) {
     return MG_OK;
 }
 
+float int_bits_as_float(int i) {
+    float f;
+    std::memcpy(&f, &i, sizeof(f));
+    return f;
+}
+
 mg_status upload_tables(mg_context *ctx) {
     const int n = ctx->n_full;
     NeighTables &nt = ctx->nt;
@@ -216,9 +222,10 @@ mg_status upload_tables(mg_context *ctx) {
             const int64_t po = p + o;
             const int64_t p2 = ((po % 2) + 2) % 2;
             const int64_t fl = po >= 0 ? po / 2 : -((-po + 1) / 2);
-            nt.lats[p][q] = static_cast<int>((p2 - p) * half + fl);
+            const int delta = static_cast<int>((p2 - p) * half + fl);
             const double *v = &ctx->offs.vec[p][3 * e];
-            nt.dsite[p][q] = make_float4((float) (2.0 * v[0]), (float) (2.0 * v[1]), (float) (2.0 * v[2]), 0.f);
+            nt.cand[p][q] = make_float4((float) (2.0 * v[0]), (float) (2.0 * v[1]), (float) (2.0 * v[2]),
+                                        int_bits_as_float(delta));
         }
     }
     set_mass_table(ctx->stream);
@@ -260,16 +267,32 @@ mg_status install_potential(mg_context *ctx, const HostPotential &hp) {
     for (int a = 0; a < 3; a++)
         for (int b = 0; b < 3; b++) put(hp.z2[HostPotential::pair_index(ele_of_type[a], ele_of_type[b])]);
     if (ctx->pot_mem) { cudaFree(ctx->pot_mem); ctx->pot_mem = nullptr; }
-    const size_t bytes = n_rec * (2 * sizeof(Knot64) + 2 * sizeof(float4));
+    // force records: pair (a, b) knot m = {z c0..c3 of pair (a, b), rho' d0..d2 of type b, 0}
+    const size_t n_zr = 9 * nr;
+    std::vector<float> zr(8 * n_zr, 0.0f);
+    for (int a = 0; a < 3; a++) {
+        for (int b = 0; b < 3; b++) {
+            const HostSpline &z = hp.z2[HostPotential::pair_index(ele_of_type[a], ele_of_type[b])];
+            const HostSpline &rb = hp.rho[ele_of_type[b]];
+            for (size_t m = 0; m < nr; m++) {
+                float *r = &zr[8 * ((a * 3 + b) * nr + m)];
+                r[0] = (float) z.c0[m]; r[1] = (float) z.c1[m]; r[2] = (float) z.c2[m]; r[3] = (float) z.c3[m];
+                r[4] = (float) rb.d0[m]; r[5] = (float) rb.d1[m]; r[6] = (float) rb.d2[m];
+            }
+        }
+    }
+    const size_t bytes = n_rec * (2 * sizeof(Knot64) + 2 * sizeof(float4)) + zr.size() * sizeof(float);
     MG_CK(cudaMalloc(&ctx->pot_mem, bytes));
     Knot64 *d_vd = static_cast<Knot64 *>(ctx->pot_mem);
     Knot64 *d_dd = d_vd + n_rec;
     float4 *d_vf = reinterpret_cast<float4 *>(d_dd + n_rec);
     float4 *d_df = d_vf + n_rec;
+    float *d_zr = reinterpret_cast<float *>(d_df + n_rec);  // 32-byte aligned: every block above is a multiple of 32 bytes
     MG_CK(cudaMemcpy(d_vd, vd.data(), n_rec * sizeof(Knot64), cudaMemcpyHostToDevice));
     MG_CK(cudaMemcpy(d_dd, dd.data(), n_rec * sizeof(Knot64), cudaMemcpyHostToDevice));
     MG_CK(cudaMemcpy(d_vf, vf.data(), n_rec * sizeof(float4), cudaMemcpyHostToDevice));
     MG_CK(cudaMemcpy(d_df, df.data(), n_rec * sizeof(float4), cudaMemcpyHostToDevice));
+    MG_CK(cudaMemcpy(d_zr, zr.data(), zr.size() * sizeof(float), cudaMemcpyHostToDevice));
 
     PotTables &pt = ctx->pt;
     pt.nr = hp.nr;
@@ -285,6 +308,7 @@ mg_status install_potential(mg_context *ctx, const HostPotential &hp) {
     pt.rho_vf = d_vf + base_rho; pt.rho_dff = d_df + base_rho;
     pt.F_vf = d_vf + base_F; pt.F_dff = d_df + base_F;
     pt.z_vf = d_vf + base_z; pt.z_dff = d_df + base_z;
+    pt.zr8 = d_zr;
     ctx->hp = hp;
     ctx->pot_ready = true;
     ctx->graph_stale = true;

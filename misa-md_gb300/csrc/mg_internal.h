@@ -120,6 +120,9 @@ struct PotTables {
     float inv_dr_f, inv_drho_f, h_inv_dr_f;   // h_inv_dr_f = (a0/2) / dr
     const Knot64 *rho_v, *rho_d, *F_v, *F_d, *z_v, *z_d;
     const float4 *rho_vf, *rho_dff, *F_vf, *F_dff, *z_vf, *z_dff;
+    // force pass, mixed form: per type pair (ti * 3 + tj) and knot one 32-byte record
+    // {r*phi c0, c1, c2, c3, rho_tj' d0, d1, d2, 0}; r*phi' comes from the value coefficients
+    const float *zr8;
 };
 
 // Per-step parameters, resident in device memory (one record per context). Kernels read dt and the
@@ -182,8 +185,9 @@ struct NeighTables {
     int nfull, npruned;
     int full[2][kMaxFull];      // reference order (inter-atom passes), linear slot offsets
     int lat[2][kMaxFull];       // gather order: entries within rc + 0.4 a0 first; linear offsets
-    int lats[2][kMaxFull];      // gather order, parity-split index deltas
-    float4 dsite[2][kMaxFull];  // gather order, site_j - site_i in units of a0/2 (w unused)
+    // gather order, mixed form: site_j - site_i in units of a0/2 (x, y, z; small exact integers) and
+    // the parity-split index delta (w, as int bits): one 16-byte constant load per candidate
+    float4 cand[2][kMaxFull];
 };
 
 // ---- kernel launchers (defined in the .cu files) ----

@@ -141,6 +141,18 @@ __device__ __forceinline__ float4 make_u4(const Geom &g, double x, double y, dou
                        __double2float_rn(__dmul_rn(__dsub_rn(z, zs), g.inv_h)), __int_as_float(type));
 }
 
+// u4 of a vacant slot: NaN coordinates, so every distance test against it fails without a type
+// check in the candidate loops; w = INVALID
+__device__ __forceinline__ float4 vacant_u4() {
+    const float nan = __int_as_float(0x7fffffff);
+    return make_float4(nan, nan, nan, __int_as_float(kInvalid));
+}
+// one 32-byte read-only load (sm_100 and later): a force record of the mixed form
+__device__ __forceinline__ void ld_nc_v8(const float *p, float (&v)[8]) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+        : "l"(p));
+}
 __device__ __forceinline__ double dt_inv_m_of(const StepParams *p, int type) {
     return type == 0 ? p->dt_inv_m[0] : (type == 1 ? p->dt_inv_m[1] : p->dt_inv_m[2]);
 }
@@ -248,7 +260,7 @@ __global__ void k_unpack_aos(Geom g, const mg_atom_element *aos, Slots s, Inter 
         const int X = t % g.Sx, r = t / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
         double xs, ys, zs;
         site_of(g, X, Y, Z, xs, ys, zs);
-        s.u4[sidx(g, t)] = make_u4(g, a.x[0], a.x[1], a.x[2], xs, ys, zs, a.type);
+        s.u4[sidx(g, t)] = a.type < 0 ? vacant_u4() : make_u4(g, a.x[0], a.x[1], a.x[2], xs, ys, zs, a.type);
         s.df32[sidx(g, t)] = (float) a.df;
     }
 }
@@ -505,13 +517,12 @@ __device__ __forceinline__ void rho_sum_mixed(const NeighTables &nt, const Geom 
     const float hinv = pt.h_inv_dr_f;
 #pragma unroll 4
     for (int q = q0; q < q1; q++) {
-        const float4 uj = __ldg(s.u4 + si + nt.lats[PAR][q]);
-        const int tj = __float_as_int(uj.w);
-        if (tj < 0) continue;
-        const float4 D = nt.dsite[PAR][q];
+        const float4 D = nt.cand[PAR][q];
+        const float4 uj = __ldg(s.u4 + si + __float_as_int(D.w));
         const float dx = (ui.x - uj.x) - D.x, dy = (ui.y - uj.y) - D.y, dz = (ui.z - uj.z) - D.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 < rc2) {
+        if (r2 < rc2) {  // false for vacancies (NaN coordinates)
+            const int tj = __float_as_int(uj.w);
             const float rp = r2 * rsqrtf(r2);
             int m; float p;
             locate_r_f(rp, hinv, pt.nr, m, p);
@@ -655,29 +666,31 @@ __device__ __forceinline__ void force_sum_mixed(const NeighTables &nt, const Geo
     const float rc2 = g.rc2_h;
     const float hinv = pt.h_inv_dr_f;
     const float inv_h = 1.0f / g.h_f;
+    const float inv_dr = pt.inv_dr_f;
     const float4 *rho_di = pt.rho_dff + ti * pt.nr;
+    const float *zr_i = pt.zr8 + 8 * (ti * 3) * pt.nr;
 #pragma unroll 2
     for (int q = q0; q < q1; q++) {
-        const int oj = si + nt.lats[PAR][q];
+        const float4 D = nt.cand[PAR][q];
+        const int oj = si + __float_as_int(D.w);
         const float4 uj = __ldg(s.u4 + oj);
-        const int tj = __float_as_int(uj.w);
-        if (tj < 0) continue;
-        const float4 D = nt.dsite[PAR][q];
         const float dx = (ui.x - uj.x) - D.x, dy = (ui.y - uj.y) - D.y, dz = (ui.z - uj.z) - D.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 < rc2) {
+        if (r2 < rc2) {  // false for vacancies (NaN coordinates)
+            const int tj = __float_as_int(uj.w);
             const float rinv_h = rsqrtf(r2);
             const float rp = r2 * rinv_h;
             int m; float p;
             locate_r_f(rp, hinv, pt.nr, m, p);
-            const float rhojp = der_f(pt.rho_dff + tj * pt.nr, m, p);
+            float z[8];  // r*phi coefficients of the pair, then rho' of type tj
+            ld_nc_v8(zr_i + 8 * (tj * pt.nr + m), z);
+            const float zv = fmaf(fmaf(fmaf(z[3], p, z[2]), p, z[1]), p, z[0]);
+            const float zp = fmaf(fmaf(3.0f * z[3], p, z[2] + z[2]), p, z[1]) * inv_dr;
+            const float rhojp = fmaf(fmaf(z[6], p, z[5]), p, z[4]);
             const float rhoip = (tj == ti) ? rhojp : der_f(rho_di, m, p);
-            const int pr = (ti * 3 + tj) * pt.nr;
-            const float zv = val_f(pt.z_vf + pr, m, p);
-            const float zp = der_f(pt.z_dff + pr, m, p);
             const float rinv = rinv_h * inv_h;
             const float phi = zv * rinv;
-            const float phip = zp * rinv - phi * rinv;
+            const float phip = (zp - phi) * rinv;
             const float psip = dfi * rhojp + __ldg(s.df32 + oj) * rhoip + phip;
             const float fpair = -psip * rinv;
             kahan(acc[0], acc[3], dx * fpair);
@@ -859,13 +872,12 @@ __device__ __forceinline__ void energy_sum_mixed(const NeighTables &nt, const Ge
                                                  float4 ui, int q0, int q1, float &sum, float &comp) {
     const float inv_h = 1.0f / g.h_f;
     for (int q = q0; q < q1; q++) {
-        const float4 uj = __ldg(s.u4 + si + nt.lats[PAR][q]);
-        const int tj = __float_as_int(uj.w);
-        if (tj < 0) continue;
-        const float4 D = nt.dsite[PAR][q];
+        const float4 D = nt.cand[PAR][q];
+        const float4 uj = __ldg(s.u4 + si + __float_as_int(D.w));
         const float dx = (ui.x - uj.x) - D.x, dy = (ui.y - uj.y) - D.y, dz = (ui.z - uj.z) - D.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 < g.rc2_h) {
+        if (r2 < g.rc2_h) {  // false for vacancies (NaN coordinates)
+            const int tj = __float_as_int(uj.w);
             const float rinv_h = rsqrtf(r2);
             int m; float p;
             locate_f(r2 * rinv_h, pt.h_inv_dr_f, pt.nr, m, p);
@@ -1056,7 +1068,7 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
                 in.df[a] = mixed ? (double) s.df32[sidx(g, sl)] : s.df[sl];
                 s.type[sl] = kInvalid;
                 s.vx[sl] = 0.0; s.vy[sl] = 0.0; s.vz[sl] = 0.0;
-                if (mixed) { float4 u = s.u4[sidx(g, sl)]; u.w = __int_as_float(kInvalid); s.u4[sidx(g, sl)] = u; }
+                if (mixed) s.u4[sidx(g, sl)] = vacant_u4();
             }
             __syncthreads();
             if (tid == 0) in.cnt[CNT_INTER] = n0 + nd;
