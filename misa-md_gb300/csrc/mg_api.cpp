@@ -267,7 +267,7 @@ mg_status install_potential(mg_context *ctx, const HostPotential &hp) {
     for (int a = 0; a < 3; a++)
         for (int b = 0; b < 3; b++) put(hp.z2[HostPotential::pair_index(ele_of_type[a], ele_of_type[b])]);
     if (ctx->pot_mem) { cudaFree(ctx->pot_mem); ctx->pot_mem = nullptr; }
-    // force records: pair (a, b) knot m = {z c0..c3 of pair (a, b), rho' d0..d2 of type b, 0}
+    // force records: pair (a, b) knot m = z c0..c3 of pair (a, b) and rho' d0..d2 of type b
     const size_t n_zr = 9 * nr;
     std::vector<float> zr(8 * n_zr, 0.0f);
     for (int a = 0; a < 3; a++) {
@@ -276,8 +276,11 @@ mg_status install_potential(mg_context *ctx, const HostPotential &hp) {
             const HostSpline &rb = hp.rho[ele_of_type[b]];
             for (size_t m = 0; m < nr; m++) {
                 float *r = &zr[8 * ((a * 3 + b) * nr + m)];
-                r[0] = (float) z.c0[m]; r[1] = (float) z.c1[m]; r[2] = (float) z.c2[m]; r[3] = (float) z.c3[m];
-                r[4] = (float) rb.d0[m]; r[5] = (float) rb.d1[m]; r[6] = (float) rb.d2[m];
+                // interleaved for a packed Horner step: {c0, d0, c1, d1, c2, d2, c3, 0}
+                r[0] = (float) z.c0[m]; r[1] = (float) rb.d0[m];
+                r[2] = (float) z.c1[m]; r[3] = (float) rb.d1[m];
+                r[4] = (float) z.c2[m]; r[5] = (float) rb.d2[m];
+                r[6] = (float) z.c3[m]; r[7] = 0.0f;
             }
         }
     }
@@ -480,6 +483,12 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     ALLOC(ctx->d_partials, (size_t) ctx->n_partials * 8);
     ALLOC(ctx->d_thermo, 8);
     ALLOC(ctx->d_sp, 1);
+    {
+        double *site_half = nullptr;
+        ctx->g.n_site_half = std::max(g.bx, std::max(2 * g.by, 2 * g.bz)) + 2;
+        ALLOC(site_half, (size_t) ctx->g.n_site_half);
+        ctx->g.site_half = site_half;
+    }
 #undef ALLOC
     e = cudaMemsetAsync(in.cnt, 0, CNT_WORDS * sizeof(int), ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(in.claim, 0x7f, ns * sizeof(int), ctx->stream);  // 0x7f7f7f7f > any list index
@@ -490,6 +499,7 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_sp, 0, sizeof(StepParams), ctx->stream);
     if (e != cudaSuccess) return fail(e);
     if (upload_tables(ctx) != MG_OK) { g_create_error = ctx->err; mg_destroy(ctx); return MG_ERR_CUDA; }
+    launch_site_table(ctx->lc(), ctx->g, const_cast<double *>(ctx->g.site_half));
     set_dt(ctx, 0.001);
     *out = ctx;
     return MG_OK;

@@ -61,6 +61,10 @@ struct Geom {
     float thr_lo_f;          // thr * (1 - 1e-4) in float: FP32 distances below it skip the exact test
     float h_f;               // a0 / 2 (float)
     float rc2_h;             // (rc / h)^2 in half-lattice units
+    // site_half[m] = RN((m / 2) a0), m in [0, n_site_half): the coordinate of half-lattice index m,
+    // rounded as the site formula of decide rounds it (x: m = i; y, z: m = 2j + parity)
+    const double *site_half;
+    int n_site_half;
 };
 
 // Lattice slot arrays (structure of arrays over every slot, ghosts included).
@@ -121,7 +125,7 @@ struct PotTables {
     const Knot64 *rho_v, *rho_d, *F_v, *F_d, *z_v, *z_d;
     const float4 *rho_vf, *rho_dff, *F_vf, *F_dff, *z_vf, *z_dff;
     // force pass, mixed form: per type pair (ti * 3 + tj) and knot one 32-byte record
-    // {r*phi c0, c1, c2, c3, rho_tj' d0, d1, d2, 0}; r*phi' comes from the value coefficients
+    // {r*phi c0, rho_tj' d0, c1, d1, c2, d2, c3, 0}; r*phi' comes from the value coefficients
     const float *zr8;
 };
 
@@ -210,6 +214,8 @@ void launch_pack_aos(const LaunchCtx &lc, const Geom &g, mg_atom_element *aos, S
 enum { PACK_ALL = 0xff, PACK_RHO = 1, PACK_DF = 2, PACK_F = 4 };
 
 void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const StepParams *sp, bool decide, bool mixed);
+// fill g.site_half (once per context)
+void launch_site_table(const LaunchCtx &lc, const Geom &g, double *site_half);
 void launch_decide_scan(const LaunchCtx &lc, const Geom &g, Slots s, Inter in);
 void launch_ghost_copy(const LaunchCtx &lc, const Geom &g, Slots s, bool mixed);
 void launch_ghost_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool mixed);

@@ -153,6 +153,46 @@ __device__ __forceinline__ void ld_nc_v8(const float *p, float (&v)[8]) {
         : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
         : "l"(p));
 }
+// Pairs of floats in one 64-bit register pair: sm_100 and later execute add/sub/mul/fma .f32x2 as
+// one instruction, each lane rounded exactly as the scalar operation.
+struct f2 {
+    unsigned long long v;
+};
+__device__ __forceinline__ f2 f2_pack(float lo, float hi) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f2 a, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
+}
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b) {
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b) {
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b) {
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+    return r;
+}
+// Kahan step on both lanes: sum += x with the compensation carried in comp
+__device__ __forceinline__ void kahan2(f2 &sum, f2 &comp, f2 x) {
+    const f2 y = f2_sub(x, comp);
+    const f2 t = f2_add(sum, y);
+    comp = f2_sub(f2_sub(t, sum), y);
+    sum = t;
+}
 __device__ __forceinline__ double dt_inv_m_of(const StepParams *p, int type) {
     return type == 0 ? p->dt_inv_m[0] : (type == 1 ? p->dt_inv_m[1] : p->dt_inv_m[2]);
 }
@@ -310,6 +350,14 @@ void launch_pack_aos(const LaunchCtx &lc, const Geom &g, mg_atom_element *aos, S
 // of atom::decide (src/atom.cpp:27-53). Displaced slots are collected unordered; the list kernel
 // sorts them into the reference's k, j, i scan order.
 // ------------------------------------------------------------------------------------------------
+__global__ void k_site_table(double a0, int n, double *out) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < n) out[m] = __dmul_rn((double) m * 0.5, a0);  // site_of: (i * 0.5) * a0, (j + half) * a0
+}
+void launch_site_table(const LaunchCtx &lc, const Geom &g, double *site_half) {
+    k_site_table<<<(g.n_site_half + 255) / 256, 256, 0, lc.stream>>>(g.a0, g.n_site_half, site_half);
+}
+
 template <bool MOVE, bool DECIDE, bool MIXED>
 __global__ void __launch_bounds__(256) k_firststep(Geom g, Slots s, Inter in, const StepParams *__restrict__ p) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -332,8 +380,10 @@ __global__ void __launch_bounds__(256) k_firststep(Geom g, Slots s, Inter in, co
         s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz;
         s.x[sl] = x; s.y[sl] = y; s.z[sl] = z;
     }
-    double xs, ys, zs;
-    site_of(g, i + g.gx, j + g.gy, k + g.gz, xs, ys, zs);
+    // the site from the table (the same rounded values site_of computes; gx is even, so the x parity
+    // of the slot is i & 1)
+    const int par = i & 1;
+    const double xs = g.site_half[i], ys = g.site_half[2 * j + par], zs = g.site_half[2 * k + par];
     const double ex = __dsub_rn(x, xs), ey = __dsub_rn(y, ys), ez = __dsub_rn(z, zs);
     const float exf = __double2float_rn(ex), eyf = __double2float_rn(ey), ezf = __double2float_rn(ez);
     if (MIXED && MOVE) {
@@ -515,11 +565,15 @@ __device__ __forceinline__ void rho_sum_mixed(const NeighTables &nt, const Geom 
                                               int q0, int q1, float &sum, float &comp) {
     const float rc2 = g.rc2_h;
     const float hinv = pt.h_inv_dr_f;
+    const f2 uixy = f2_pack(ui.x, ui.y);
 #pragma unroll 4
     for (int q = q0; q < q1; q++) {
         const float4 D = nt.cand[PAR][q];
         const float4 uj = __ldg(s.u4 + si + __float_as_int(D.w));
-        const float dx = (ui.x - uj.x) - D.x, dy = (ui.y - uj.y) - D.y, dz = (ui.z - uj.z) - D.z;
+        const f2 dxy = f2_sub(f2_sub(uixy, f2_pack(uj.x, uj.y)), f2_pack(D.x, D.y));
+        const float dz = (ui.z - uj.z) - D.z;
+        float dx, dy;
+        f2_unpack(dxy, dx, dy);
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (r2 < rc2) {  // false for vacancies (NaN coordinates)
             const int tj = __float_as_int(uj.w);
@@ -662,19 +716,23 @@ __global__ void __launch_bounds__(512) k_lat_force_fp64(const __grid_constant__ 
 
 template <int PAR>
 __device__ __forceinline__ void force_sum_mixed(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int si, int ti,
-                                                float4 ui, float dfi, int q0, int q1, float acc[6]) {
+                                                float4 ui, float dfi, int q0, int q1, f2 &sxy, f2 &cxy, float &sz, float &cz) {
     const float rc2 = g.rc2_h;
     const float hinv = pt.h_inv_dr_f;
     const float inv_h = 1.0f / g.h_f;
     const float inv_dr = pt.inv_dr_f;
     const float4 *rho_di = pt.rho_dff + ti * pt.nr;
     const float *zr_i = pt.zr8 + 8 * (ti * 3) * pt.nr;
+    const f2 uixy = f2_pack(ui.x, ui.y);
 #pragma unroll 2
     for (int q = q0; q < q1; q++) {
         const float4 D = nt.cand[PAR][q];
         const int oj = si + __float_as_int(D.w);
         const float4 uj = __ldg(s.u4 + oj);
-        const float dx = (ui.x - uj.x) - D.x, dy = (ui.y - uj.y) - D.y, dz = (ui.z - uj.z) - D.z;
+        const f2 dxy = f2_sub(f2_sub(uixy, f2_pack(uj.x, uj.y)), f2_pack(D.x, D.y));
+        const float dz = (ui.z - uj.z) - D.z;
+        float dx, dy;
+        f2_unpack(dxy, dx, dy);
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (r2 < rc2) {  // false for vacancies (NaN coordinates)
             const int tj = __float_as_int(uj.w);
@@ -682,25 +740,29 @@ __device__ __forceinline__ void force_sum_mixed(const NeighTables &nt, const Geo
             const float rp = r2 * rinv_h;
             int m; float p;
             locate_r_f(rp, hinv, pt.nr, m, p);
-            float z[8];  // r*phi coefficients of the pair, then rho' of type tj
+            // record {c0, d0, c1, d1, c2, d2, c3, 0}: r*phi = c(p), rho_tj' = d(p), both in one Horner
+            float z[8];
             ld_nc_v8(zr_i + 8 * (tj * pt.nr + m), z);
-            const float zv = fmaf(fmaf(fmaf(z[3], p, z[2]), p, z[1]), p, z[0]);
-            const float zp = fmaf(fmaf(3.0f * z[3], p, z[2] + z[2]), p, z[1]) * inv_dr;
-            const float rhojp = fmaf(fmaf(z[6], p, z[5]), p, z[4]);
+            const f2 pp = f2_pack(p, p);
+            f2 h = f2_fma(f2_pack(z[6], z[7]), pp, f2_pack(z[4], z[5]));
+            h = f2_fma(h, pp, f2_pack(z[2], z[3]));
+            h = f2_fma(h, pp, f2_pack(z[0], z[1]));
+            float zv, rhojp;
+            f2_unpack(h, zv, rhojp);
+            const float zp = fmaf(fmaf(3.0f * z[6], p, z[4] + z[4]), p, z[2]) * inv_dr;
             const float rhoip = (tj == ti) ? rhojp : der_f(rho_di, m, p);
             const float rinv = rinv_h * inv_h;
             const float phi = zv * rinv;
             const float phip = (zp - phi) * rinv;
             const float psip = dfi * rhojp + __ldg(s.df32 + oj) * rhoip + phip;
             const float fpair = -psip * rinv;
-            kahan(acc[0], acc[3], dx * fpair);
-            kahan(acc[1], acc[4], dy * fpair);
-            kahan(acc[2], acc[5], dz * fpair);
+            kahan2(sxy, cxy, f2_mul(dxy, f2_pack(fpair, fpair)));
+            kahan(sz, cz, dz * fpair);
         }
     }
 }
 
-__global__ void __launch_bounds__(512) k_lat_force_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, StepParams *sp,
+__global__ void __launch_bounds__(512, 3) k_lat_force_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, StepParams *sp,
                                                          bool kick, bool hook, int order) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     int par;
@@ -711,19 +773,24 @@ __global__ void __launch_bounds__(512) k_lat_force_mixed(const __grid_constant__
     const int ti = __float_as_int(ui.w);
     if (ti < 0) { s.fx[sl] = 0.0; s.fy[sl] = 0.0; s.fz[sl] = 0.0; return; }
     const float dfi = s.df32[si];
-    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // sums x, y, z and their Kahan compensations
+    // force sums (x and y packed, z) with their Kahan compensations
+    f2 sxy = f2_pack(0.f, 0.f), cxy = f2_pack(0.f, 0.f);
+    float sz = 0.f, cz = 0.f;
     const int np = nt.npruned;
-    if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, 0, np, acc);
-    else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, 0, np, acc);
+    if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, 0, np, sxy, cxy, sz, cz);
+    else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, 0, np, sxy, cxy, sz, cz);
     if (in.far_flag[sl]) {
         const int nf = nt.nfull;
-        if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, np, nf, acc);
-        else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, np, nf, acc);
+        if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, np, nf, sxy, cxy, sz, cz);
+        else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, np, nf, sxy, cxy, sz, cz);
     }
+    float sx, sy, cx, cy;
+    f2_unpack(sxy, sx, sy);
+    f2_unpack(cxy, cx, cy);
     const double h = 0.5 * g.a0;
-    const double fx = h * ((double) acc[0] - (double) acc[3]);
-    const double fy = h * ((double) acc[1] - (double) acc[4]);
-    const double fz = h * ((double) acc[2] - (double) acc[5]);
+    const double fx = h * ((double) sx - (double) cx);
+    const double fy = h * ((double) sy - (double) cy);
+    const double fz = h * ((double) sz - (double) cz);
     s.fx[sl] = fx; s.fy[sl] = fy; s.fz[sl] = fz;
     if (kick && !hook && lattice_only(in)) {
         const double c = dt_inv_m_of(sp, ti);
