@@ -232,6 +232,18 @@ void *mg_batch_stream(const mg_batch *b);
 const char *mg_batch_last_error(const mg_batch *b);
 mg_status mg_batch_destroy(mg_batch *b);
 
+/* ---- Creation mode (simulation::createAtoms with create_mode, src/simulation.cpp:57-84 ->
+ * WorldBuilder::build, src/world_builder.cpp:64-199), host only ----
+ * Fills a host slot array (n_slots = the grid of mg_grid for this box) with the reference's
+ * created crystal: ids 1..N in k, j, i order, types drawn with the C library's rand() in its
+ * default state against alloy_ratio (Fe, Cu, Ni), positions on the BCC sites, velocities
+ * (u - 0.5) / m from md_rand's engine seeded with seed, zero total momentum, then rescaled to t_set
+ * (t_set == 0: no rescale). rng selects the engine the reference build chose with MD_RAND. */
+enum { MG_RNG_MT = 0, MG_RNG_LCG = 1, MG_RNG_STC = 2, MG_RNG_LEGACY = 3 };
+mg_status mg_world_build(const int64_t phase_space[3], double lattice_const, double cutoff_radius_factor,
+                         double t_set, uint32_t seed, const int32_t alloy_ratio[3], int32_t rng,
+                         mg_atom_element *atoms, int64_t n_slots);
+
 /* Page-lock a host range (the caller's slot array) so mg_step_host / mg_upload / mg_download copy it
  * by DMA; undo with mg_host_unregister before freeing it. */
 mg_status mg_host_register(void *ptr, uint64_t bytes);

@@ -92,6 +92,7 @@ _PROTOS = {
     "mg_kernel_times": (_I32, [_P, _P, _I32, _P, _P]),
     "mg_launches_per_step": (_I32, [_P, _P]),
     "mg_stream": (_P, [_P]),
+    "mg_world_build": (_I32, [_P, _D, _D, _D, ctypes.c_uint32, _P, _I32, _P, _I64]),
     "mg_batch_create": (_I32, [_P, _I32, _I32, _P]),
     "mg_batch_run": (_I32, [_P, _I64, _I32]),
     "mg_batch_launches_per_step": (_I32, [_P, _P]),
@@ -135,6 +136,24 @@ def exported_symbols():
 
 def _ptr(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+RNG = {"mt": 0, "lcg": 1, "stc": 2, "legacy": 3}
+
+
+def world_build(cells, lattice_const, cutoff_radius_factor, t_set, seed, alloy_ratio=(1, 0, 0), rng="mt"):
+    """The reference's creation mode (WorldBuilder::build): returns the host slot array of the
+    ghost-extended grid, equal to the reference's for the same seed, alloy ratio and MD_RAND engine."""
+    lib = load_library()
+    Sx, Sy, Sz, _, _, _ = workloads.grid(cells, cutoff_radius_factor)
+    atoms = np.zeros(Sx * Sy * Sz, dtype=ATOM_DTYPE)
+    ps = np.asarray(cells, dtype=np.int64)
+    ratio = np.asarray(alloy_ratio, dtype=np.int32)
+    st = lib.mg_world_build(_ptr(ps), float(lattice_const), float(cutoff_radius_factor), float(t_set), int(seed),
+                            _ptr(ratio), RNG[rng], _ptr(atoms), atoms.size)
+    if st != 0:
+        raise MgError(st, (lib.mg_last_error(None) or b"").decode())
+    return atoms
 
 
 def host_register(array):
@@ -423,8 +442,14 @@ class Simulation:
         self.ctx = Context(self.phase_space, lattice_const, cutoff_radius_factor, self.precision,
                            self.inter_capacity)
 
-    def create_atoms(self, init_step_len, t_set, create_seed, alloy_ratio=(1.0, 0.0, 0.0), atoms=None):
-        """Create-mode state (WorldBuilder-style BCC crystal at t_set) unless a slot array is given."""
+    def create_atoms(self, init_step_len, t_set, create_seed, alloy_ratio=(1.0, 0.0, 0.0), atoms=None,
+                     builder="maxwell", rng="mt"):
+        """Create-mode state unless a slot array is given. builder "worldbuilder" reproduces the
+        reference's WorldBuilder::build bit for bit (integer alloy ratios, rng = the MD_RAND engine);
+        "maxwell" draws Maxwell velocities and exact alloy counts from the seed."""
+        if atoms is None and builder == "worldbuilder":
+            atoms = world_build(self.phase_space, self.lattice_const, self.cutoff_radius_factor, t_set, create_seed,
+                                tuple(int(r) for r in alloy_ratio), rng)
         if atoms is None:
             total = float(sum(alloy_ratio))
             atoms = workloads.build_state(self.phase_space, self.lattice_const, self.cutoff_radius_factor,

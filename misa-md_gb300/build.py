@@ -14,7 +14,7 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libmisa_gb300.so")
-SOURCES = ["csrc/mg_kernels.cu", "csrc/mg_api.cpp", "csrc/mg_potential.cpp", "csrc/mg_noalloc.cu"]
+SOURCES = ["csrc/mg_kernels.cu", "csrc/mg_api.cpp", "csrc/mg_potential.cpp", "csrc/mg_noalloc.cu", "csrc/mg_world.cpp"]
 HEADERS = ["csrc/mg_internal.h", "../include/misa_gb300.h"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC,-ffp-contract=off"]

@@ -38,6 +38,7 @@
 #include <cstring>
 #include <fstream>
 #include <list>
+#include <random>
 #include <sstream>
 #include <string>
 #include <unordered_map>
@@ -902,6 +903,57 @@ struct orc_sim {
         for (orc_atom &a : inter_list) { a.v[0] *= f; a.v[1] *= f; a.v[2] *= f; }
     }
 
+    // ---- WorldBuilder::build (src/world_builder.cpp:64-199), one rank ----
+    // Velocities from md_rand::random() = rand32() * (1.0 / rng.max()) of the engine the build chose
+    // (src/utils/random/random.cpp:31-37, rand_generators.cpp); types from the C library's rand(),
+    // which the reference leaves in its default state (srand(1) restores it here).
+    template <class Engine>
+    void world_build_with(Engine &rng, double rng_max, double t_set, const int32_t ratio[3]) {
+        std::srand(1);
+        const Domain &d = dom;
+        int ratio_total = 0;
+        for (int t = 0; t < 3; t++) ratio_total += ratio[t];
+        uint64_t id_pre = 0;
+        foreach_sub_box([&](orc_atom &a, int64_t x, int64_t y, int64_t z) {
+            const int64_t i = x - d.dbx_ghost[0], j = y - d.dbx_ghost[1], k = z - d.dbx_ghost[2];
+            a.id = ++id_pre;
+            const int r = std::rand() % ratio_total;  // randomAtomsType
+            int rank_local = 0;
+            for (int t = 0; t < 3; t++) {
+                rank_local += ratio[t];
+                if (r < rank_local) { a.type = t; break; }
+            }
+            const double mass = atom_mass(a.type);
+            a.x[0] = (i * 0.5) * dom.a0;
+            a.x[1] = j * dom.a0 + (i % 2) * (dom.a0 / 2);
+            a.x[2] = k * dom.a0 + (i % 2) * (dom.a0 / 2);
+            a.v[0] = (static_cast<double>(rng()) * (1.0 / rng_max) - 0.5) / mass;
+            a.v[1] = (static_cast<double>(rng()) * (1.0 / rng_max) - 0.5) / mass;
+            a.v[2] = (static_cast<double>(rng()) * (1.0 / rng_max) - 0.5) / mass;
+        });
+        double p[4] = {0.0, 0.0, 0.0, 0.0};
+        foreach_sub_box([&](orc_atom &a, int64_t, int64_t, int64_t) {
+            const double m = atom_mass(a.type);
+            p[0] += a.v[0] * m;
+            p[1] += a.v[1] * m;
+            p[2] += a.v[2] * m;
+            p[3] += m;
+        });
+        const uint64_t n = 2 * static_cast<uint64_t>(d.sub_size[0] * d.sub_size[1] * d.sub_size[2]);
+        if (p[3] > 0.0) {
+            p[0] /= n;
+            p[1] /= n;
+            p[2] /= n;
+        }
+        foreach_sub_box([&](orc_atom &a, int64_t, int64_t, int64_t) {
+            const double m = atom_mass(a.type);
+            a.v[0] -= (p[0] / m);
+            a.v[1] -= (p[1] / m);
+            a.v[2] -= (p[2] / m);
+        });
+        if (t_set != 0.0) rescale(t_set, n);
+    }
+
     // ---- per-atom potential energy (extension; follows computeEam's loop structure) ----
     double potential_energy(double *per_slot, double *per_inter, int64_t inter_cap) {
         std::vector<double> e(n_slots(), 0.0);
@@ -1167,6 +1219,30 @@ void orc_collision_step(orc_sim *s, const int32_t lat[4], const double dir[3], d
     s->exchange_atom();
     s->clear_force();
     s->compute_eam();
+}
+
+// LegacyRand (src/utils/random/legacy_random.hpp): Park-Miller minimal standard with Schrage's method
+struct OrcLegacyRand {
+    int32_t s;
+    uint32_t operator()() {
+        const int32_t k = s / 127773;
+        s = 16807 * (s - k * 127773) - 2836 * k;
+        if (s < 0) s += 0x7fffffff;
+        return static_cast<uint32_t>(s);
+    }
+};
+
+int32_t orc_world_build(orc_sim *s, double t_set, uint32_t seed, const int32_t ratio[3], int32_t rng) {
+    for (auto &a : s->atoms) { a = orc_atom{}; a.type = kInvalid; }
+    s->inter_list.clear();
+    switch (rng) {
+        case 0: { std::mt19937 e(seed); s->world_build_with(e, static_cast<double>(std::mt19937::max()), t_set, ratio); break; }
+        case 1: { std::minstd_rand e(seed); s->world_build_with(e, static_cast<double>(std::minstd_rand::max()), t_set, ratio); break; }
+        case 2: { std::ranlux24 e(seed); s->world_build_with(e, static_cast<double>(std::ranlux24::max()), t_set, ratio); break; }
+        case 3: { OrcLegacyRand e{static_cast<int32_t>(seed)}; s->world_build_with(e, 2147483647.0, t_set, ratio); break; }
+        default: return 1;
+    }
+    return 0;
 }
 
 double orc_mvv(const orc_sim *s) { return const_cast<orc_sim *>(s)->mvv(); }

@@ -110,6 +110,10 @@ void orc_collision_step(orc_sim *s, const int32_t lat[4], const double dir[3], d
 void orc_setv(orc_sim *s, const int32_t lat[4], const double dir[3], double energy_ev);
 
 /* Thermo (src/system_configuration.cpp). */
+/* WorldBuilder::build (src/world_builder.cpp:64-199) into the simulation's slots: rng 0 mt19937,
+ * 1 minstd_rand, 2 ranlux24, 3 LegacyRand (the MD_RAND choices); atom types from the C library's
+ * rand() in its default state. Returns 0, or 1 for an unknown rng. */
+int32_t orc_world_build(orc_sim *s, double t_set, uint32_t seed, const int32_t ratio[3], int32_t rng);
 double orc_mvv(const orc_sim *s);
 double orc_kinetic_energy(const orc_sim *s);
 double orc_temperature(const orc_sim *s, uint64_t n_atoms);

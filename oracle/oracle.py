@@ -74,6 +74,7 @@ _PROTOS = {
     "orc_simulate": (None, [_P, _I64]),
     "orc_collision_step": (None, [_P, _P, _P, _D]),
     "orc_setv": (None, [_P, _P, _P, _D]),
+    "orc_world_build": (_I32, [_P, _D, ctypes.c_uint32, _P, _I32]),
     "orc_mvv": (_D, [_P]),
     "orc_kinetic_energy": (_D, [_P]),
     "orc_temperature": (_D, [_P, _U64]),
@@ -252,6 +253,11 @@ class OracleSim:
         lat = np.asarray(lat, dtype=np.int32)
         d = np.asarray(direction, dtype=np.float64)
         self.L.orc_setv(self.h, _ptr(lat), _ptr(d), float(energy))
+
+    def world_build(self, t_set, seed, ratio=(1, 0, 0), rng=0):
+        r = np.asarray(ratio, dtype=np.int32)
+        if self.L.orc_world_build(self.h, float(t_set), int(seed), _ptr(r), int(rng)) != 0:
+            raise ValueError("unknown random engine")
 
     def system_force(self):
         out = np.zeros(3)
