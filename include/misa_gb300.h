@@ -213,6 +213,38 @@ mg_status mg_launches_per_step(const mg_context *ctx, int32_t *n);
 /* CUDA stream of the context (a cudaStream_t), for callers timing on it. */
 void *mg_stream(const mg_context *ctx);
 
+/* ---- Stage machine (MDSimulation::beforeStep / postStep, frontend/md_simulation.cpp:40-111) ----
+ * Runs `steps` loop bodies through a list of stages as the reference's driver does: when the current
+ * stage's steps are used up (checked once per step), the next stage starts and sets its dt
+ * (step_length 0: default_dt); a stage with collision_set applies its PKA (simulation::collisionStep)
+ * before stage step collision_step - 1 (the reference does so only when an origin dump path is
+ * configured); a stage with rescales_set rescales to rescale_t every rescale_every stage steps
+ * (configuration::rescale, n_atoms global atoms). Everything is enqueued on the context's stream;
+ * the host waits once, at the end. Every thermo_interval steps (0: none) one sample is recorded:
+ * steps taken since creation, simulated time, sum m v^2 and temperature (configuration::temperature).
+ * Running out of stages returns MG_ERR_STATE (the reference aborts). */
+typedef struct mg_stage {
+    int64_t steps;
+    double step_length;       /* ps; 0 = default_dt */
+    int32_t collision_set;
+    int32_t rescales_set;
+    int64_t collision_step;   /* 1-based stage step of the collision */
+    int32_t collision_lat[4]; /* unit cell x, y, z and basis (0 corner, 1 centre) */
+    double direction[3];
+    double pka_energy;        /* eV */
+    double rescale_t;         /* K */
+    int64_t rescale_every;
+} mg_stage;
+typedef struct mg_thermo_sample {
+    int64_t step;
+    double time_ps;
+    double mvv;
+    double temperature;
+} mg_thermo_sample;
+mg_status mg_run_stages(mg_context *ctx, const mg_stage *stages, int32_t n_stages, int64_t steps, double default_dt,
+                        int64_t n_atoms, int32_t thermo_interval, mg_thermo_sample *samples, int64_t cap,
+                        int64_t *n_samples);
+
 /* ---- Batched independent replicas (extension, no reference counterpart: the reference runs one
  * simulation per MPI job). One CUDA graph holds the loop body (mg_simulate's step) of every context
  * as its own branch, steps_per_launch bodies deep, so one graph launch advances all replicas; their

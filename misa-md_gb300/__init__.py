@@ -51,6 +51,18 @@ class ThermoOut(ctypes.Structure):
                 ("device_errors", ctypes.c_uint32), ("pad_", ctypes.c_uint32)]
 
 
+class StageIn(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int64), ("step_length", ctypes.c_double), ("collision_set", ctypes.c_int32),
+                ("rescales_set", ctypes.c_int32), ("collision_step", ctypes.c_int64),
+                ("collision_lat", ctypes.c_int32 * 4), ("direction", ctypes.c_double * 3),
+                ("pka_energy", ctypes.c_double), ("rescale_t", ctypes.c_double), ("rescale_every", ctypes.c_int64)]
+
+
+class ThermoSample(ctypes.Structure):
+    _fields_ = [("step", ctypes.c_int64), ("time_ps", ctypes.c_double), ("mvv", ctypes.c_double),
+                ("temperature", ctypes.c_double)]
+
+
 _LIB = None
 _P = ctypes.c_void_p
 _I32, _I64, _U64, _D = ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64, ctypes.c_double
@@ -93,6 +105,7 @@ _PROTOS = {
     "mg_launches_per_step": (_I32, [_P, _P]),
     "mg_stream": (_P, [_P]),
     "mg_world_build": (_I32, [_P, _D, _D, _D, ctypes.c_uint32, _P, _I32, _P, _I64]),
+    "mg_run_stages": (_I32, [_P, _P, _I32, _I64, _D, _I64, _I32, _P, _I64, _P]),
     "mg_batch_create": (_I32, [_P, _I32, _I32, _P]),
     "mg_batch_run": (_I32, [_P, _I64, _I32]),
     "mg_batch_launches_per_step": (_I32, [_P, _P]),
@@ -250,6 +263,35 @@ class Context:
     def set_variable_timestep(self, dx_max, dt_min, dt_max):
         """dt = clamp(dx_max / max|v|, dt_min, dt_max) before every step (Angstrom, ps)."""
         self._check(self.lib.mg_set_variable_timestep(self.h, float(dx_max), float(dt_min), float(dt_max)))
+
+    def run_stages(self, stages, steps, default_dt, n_atoms, thermo_interval=0):
+        """The reference's stage driver (MDSimulation::beforeStep / postStep) on the device. stages: dicts
+        with steps, step_length, and optionally collision_step + lat + direction + energy and
+        rescale_t + rescale_every. Returns the thermo samples as dicts."""
+        arr = (StageIn * max(1, len(stages)))()
+        for k, st in enumerate(stages):
+            a = arr[k]
+            a.steps = int(st["steps"])
+            a.step_length = float(st.get("step_length", 0.0))
+            if "collision_step" in st:
+                a.collision_set = 1
+                a.collision_step = int(st["collision_step"])
+                for i in range(4):
+                    a.collision_lat[i] = int(st["lat"][i])
+                for i in range(3):
+                    a.direction[i] = float(st["direction"][i])
+                a.pka_energy = float(st["energy"])
+            if "rescale_t" in st:
+                a.rescales_set = 1
+                a.rescale_t = float(st["rescale_t"])
+                a.rescale_every = int(st["rescale_every"])
+        cap = steps // thermo_interval if thermo_interval else 0
+        out = (ThermoSample * max(1, cap))()
+        n = ctypes.c_int64(0)
+        self._check(self.lib.mg_run_stages(self.h, arr, len(stages), int(steps), float(default_dt), int(n_atoms),
+                                           int(thermo_interval), out, cap, ctypes.byref(n)))
+        return [{"step": out[k].step, "time_ps": out[k].time_ps, "mvv": out[k].mvv,
+                 "temperature": out[k].temperature} for k in range(n.value)]
 
     def clock(self):
         """(steps taken, simulated time in ps, dt of the last step)."""

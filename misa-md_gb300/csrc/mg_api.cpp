@@ -59,6 +59,8 @@ struct mg_context {
     mg_atom_element *d_aos = nullptr;
     double *d_partials = nullptr;
     double *d_thermo = nullptr;
+    double *d_samples = nullptr;    // stage-machine thermo samples (8 doubles each)
+    int64_t n_samples_cap = 0;
     int n_partials = 0;
     double *d_ws_xyz = nullptr;
     int64_t *d_ws_coords = nullptr, *d_ws_index = nullptr;
@@ -414,6 +416,7 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     g.inv_h_f = (float) g.inv_h;
     g.thr_lo_f = (float) (g.thr * (1.0 - 1e-4));
     g.rc2_h = (float) (g.rc2 * g.inv_h * g.inv_h);
+    g.rc2_pre = (float) ((double) g.rc2_h * (1.0 + 1e-4));
 
     // offset tables, and the lattice gather order: pruned entries (site distance below
     // rc + 0.4 a0, with margin) first, in reference order, then the rest
@@ -870,10 +873,8 @@ mg_status mg_phase(mg_context *ctx, int32_t phase) {
     return status_from_bits(ctx, bits);
 }
 
-mg_status mg_collision_step(mg_context *ctx, const int32_t lat[4], const double dir[3], double energy) {
-    if (!ctx || !lat || !dir) return MG_ERR_ARG;
-    mg_status st = require_ready(ctx);
-    if (st != MG_OK) return st;
+// simulation::collisionStep (src/simulation.cpp:282-291) enqueued on the context's stream
+static mg_status enqueue_collision(mg_context *ctx, const int32_t lat[4], const double dir[3], double energy) {
     // atom::setv bounds (src/atom.cpp:477-482), one rank: the sub-box starts at 0
     const Geom &g = ctx->g;
     if (lat[3] < 0 || lat[3] > 1) { ctx->err = "PKA basis index must be 0 or 1"; return MG_ERR_ARG; }
@@ -884,10 +885,17 @@ mg_status mg_collision_step(mg_context *ctx, const int32_t lat[4], const double 
         ctx->vmax_stale = true;
     }
     // exchangeInter, borderInter (the ghost list is not cleared here, as in the reference),
-    // exchangeAtom, clearForce, computeEam (src/simulation.cpp:282-291)
+    // exchangeAtom, clearForce, computeEam
     launch_inter_manage(ctx->lc(), g, ctx->s, ctx->in, MANAGE_EXCHANGE | MANAGE_BORDER, ctx->mixed());
     seq_compute_eam(ctx, false, false, 0, nullptr);
-    if ((st = check_launch(ctx)) != MG_OK) return st;
+    return check_launch(ctx);
+}
+
+mg_status mg_collision_step(mg_context *ctx, const int32_t lat[4], const double dir[3], double energy) {
+    if (!ctx || !lat || !dir) return MG_ERR_ARG;
+    mg_status st = require_ready(ctx);
+    if (st != MG_OK) return st;
+    if ((st = enqueue_collision(ctx, lat, dir, energy)) != MG_OK) return st;
     uint32_t bits = 0;
     if ((st = read_device_errors(ctx, &bits)) != MG_OK) return st;
     ctx->energy_valid = false;
@@ -903,6 +911,89 @@ mg_status mg_rescale(mg_context *ctx, double t_set, uint64_t n_atoms) {
     if (st != MG_OK) return st;
     MG_CK(cudaStreamSynchronize(ctx->stream));
     return MG_OK;
+}
+
+// MDSimulation::beforeStep / postStep (frontend/md_simulation.cpp:40-111) around the loop body, all on
+// the context's stream: stage changes set dt on the device, rescales and PKAs are kernels, steps are
+// graph replays, thermo samples go to a device buffer read once at the end.
+mg_status mg_run_stages(mg_context *ctx, const mg_stage *stages, int32_t n_stages, int64_t steps, double default_dt,
+                        int64_t n_atoms, int32_t thermo_interval, mg_thermo_sample *samples, int64_t cap,
+                        int64_t *n_samples) {
+    if (!ctx || n_stages < 0 || (n_stages > 0 && !stages) || steps < 0 || n_atoms < 2 || thermo_interval < 0 ||
+        cap < 0 || (cap > 0 && !samples) || !(default_dt > 0))
+        return MG_ERR_ARG;
+    if (!ctx->prepared) { ctx->err = "mg_prepare must run before mg_run_stages"; return MG_ERR_STATE; }
+    for (int32_t k = 0; k < n_stages; k++) {
+        const mg_stage &st = stages[k];
+        if (st.steps < 0 || st.step_length < 0 || (st.rescales_set && (st.rescale_every < 1 || !(st.rescale_t > 0))) ||
+            (st.collision_set && (st.collision_lat[3] < 0 || st.collision_lat[3] > 1))) {
+            ctx->err = "stage " + std::to_string(k) + ": bad parameters";
+            return MG_ERR_ARG;
+        }
+    }
+    const int64_t want = thermo_interval ? steps / thermo_interval : 0;
+    if (want > cap) { ctx->err = "sample buffer smaller than steps / thermo_interval"; return MG_ERR_ARG; }
+    constexpr int kWords = 8;  // thermo words 0..5, steps, time
+    if (want > ctx->n_samples_cap) {
+        MG_CK(dalloc(ctx, &ctx->d_samples, static_cast<size_t>(want) * kWords));
+        ctx->n_samples_cap = want;
+    }
+    mg_status st;
+    if ((st = build_graph(ctx)) != MG_OK) return st;
+    const LaunchCtx lc = ctx->lc();
+    int64_t cur_stage_steps = 0, stage_len = 0, taken = 0;
+    int32_t next = 0;
+    const mg_stage *cur = nullptr;
+    for (int64_t step = 0; step < steps; step++) {
+        if (cur_stage_steps >= stage_len) {  // one stage change per step at most, as the reference does
+            if (next >= n_stages) {
+                ctx->err = "no more stages at step " + std::to_string(step);
+                cudaStreamSynchronize(ctx->stream);
+                return MG_ERR_STATE;
+            }
+            cur = &stages[next++];
+            stage_len = cur->steps;
+            cur_stage_steps = 0;
+            set_dt(ctx, cur->step_length == 0.0 ? default_dt : cur->step_length);
+        }
+        if (cur->collision_set && cur_stage_steps + 1 == cur->collision_step) {
+            if ((st = enqueue_collision(ctx, cur->collision_lat, cur->direction, cur->pka_energy)) != MG_OK) return st;
+        }
+        if (cur->rescales_set && cur_stage_steps % cur->rescale_every == 0) {
+            launch_thermo(lc, ctx->g, ctx->s, ctx->in, false, ctx->d_partials, ctx->n_partials, ctx->d_thermo);
+            launch_rescale(lc, ctx->g, ctx->s, ctx->in, ctx->d_thermo, cur->rescale_t, static_cast<uint64_t>(n_atoms));
+            ctx->vmax_stale = true;
+        }
+        if (ctx->vmax_stale) {
+            launch_vmax_full(lc, ctx->g, ctx->s, ctx->in, ctx->d_sp);
+            ctx->vmax_stale = false;
+        }
+        MG_CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+        cur_stage_steps++;
+        if (thermo_interval && (step + 1) % thermo_interval == 0) {
+            double *rec = ctx->d_samples + kWords * taken;
+            launch_thermo(lc, ctx->g, ctx->s, ctx->in, false, ctx->d_partials, ctx->n_partials, rec);
+            launch_clock_sample(lc, ctx->d_sp, rec + 6);
+            taken++;
+        }
+    }
+    if ((st = check_launch(ctx)) != MG_OK) return st;
+    std::vector<double> h(static_cast<size_t>(taken) * kWords);
+    if (taken) MG_CK(cudaMemcpyAsync(h.data(), ctx->d_samples, h.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_CK(cudaStreamSynchronize(ctx->stream));
+    const double to_t = kMvv2e / (static_cast<double>(3 * n_atoms - 3) * kBoltz);
+    for (int64_t k = 0; k < taken; k++) {
+        const double *r = &h[kWords * k];
+        samples[k].step = static_cast<int64_t>(r[6]);
+        samples[k].time_ps = r[7];
+        samples[k].mvv = r[0];
+        samples[k].temperature = r[0] * to_t;
+    }
+    if (n_samples) *n_samples = taken;
+    ctx->energy_valid = false;
+    uint32_t bits = 0;
+    if ((st = read_device_errors(ctx, &bits)) != MG_OK) return st;
+    return status_from_bits(ctx, bits);
 }
 
 mg_status mg_thermo(mg_context *ctx, int32_t with_energy, mg_thermo_out *out) {

@@ -61,6 +61,7 @@ struct Geom {
     float thr_lo_f;          // thr * (1 - 1e-4) in float: FP32 distances below it skip the exact test
     float h_f;               // a0 / 2 (float)
     float rc2_h;             // (rc / h)^2 in half-lattice units
+    float rc2_pre;           // rc2_h * (1 + 1e-4): FP32 candidate test of the FP64 gathers
     // site_half[m] = RN((m / 2) a0), m in [0, n_site_half): the coordinate of half-lattice index m,
     // rounded as the site formula of decide rounds it (x: m = i; y, z: m = 2j + parity)
     const double *site_half;
@@ -226,6 +227,8 @@ void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, Pot
 void launch_secondstep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams *sp, bool lattice);
 // step head: records the step's dt and, in variable mode, sets dt from the last kick's max |v|
 void launch_step_head(const LaunchCtx &lc, StepParams *sp);
+// out[0] = steps taken, out[1] = simulated time
+void launch_clock_sample(const LaunchCtx &lc, const StepParams *sp, double *out);
 // set the timestep rule and dt / dt/(2m) (dx_max <= 0: fixed dt)
 void launch_set_step(const LaunchCtx &lc, StepParams *sp, double dt, double dx_max, double dt_min, double dt_max);
 // recompute the max |v|^2 words from the state (after uploads, setv, rescale, single phases)

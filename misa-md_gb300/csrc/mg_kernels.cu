@@ -296,13 +296,13 @@ __global__ void k_unpack_aos(Geom g, const mg_atom_element *aos, Slots s, Inter 
     s.rho[t] = a.rho; s.df[t] = a.df;
     s.type[t] = (int8_t) a.type;
     s.id[t] = a.id;
-    if (mixed) {
+    {  // u4 in both precisions: the gathers' FP32 candidate test reads it
         const int X = t % g.Sx, r = t / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
         double xs, ys, zs;
         site_of(g, X, Y, Z, xs, ys, zs);
         s.u4[sidx(g, t)] = a.type < 0 ? vacant_u4() : make_u4(g, a.x[0], a.x[1], a.x[2], xs, ys, zs, a.type);
-        s.df32[sidx(g, t)] = (float) a.df;
     }
+    if (mixed) s.df32[sidx(g, t)] = (float) a.df;
 }
 
 __global__ void k_pack_aos(Geom g, mg_atom_element *aos, Slots s, int fields, bool mixed) {
@@ -358,7 +358,7 @@ void launch_site_table(const LaunchCtx &lc, const Geom &g, double *site_half) {
     k_site_table<<<(g.n_site_half + 255) / 256, 256, 0, lc.stream>>>(g.a0, g.n_site_half, site_half);
 }
 
-template <bool MOVE, bool DECIDE, bool MIXED>
+template <bool MOVE, bool DECIDE>
 __global__ void __launch_bounds__(256) k_firststep(Geom g, Slots s, Inter in, const StepParams *__restrict__ p) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= g.n_local) return;
@@ -386,7 +386,7 @@ __global__ void __launch_bounds__(256) k_firststep(Geom g, Slots s, Inter in, co
     const double xs = g.site_half[i], ys = g.site_half[2 * j + par], zs = g.site_half[2 * k + par];
     const double ex = __dsub_rn(x, xs), ey = __dsub_rn(y, ys), ez = __dsub_rn(z, zs);
     const float exf = __double2float_rn(ex), eyf = __double2float_rn(ey), ezf = __double2float_rn(ez);
-    if (MIXED && MOVE) {
+    if (MOVE) {
         const float ih = g.inv_h_f;
         s.u4[sidx(g, sl)] = make_float4(exf * ih, eyf * ih, ezf * ih, __int_as_float(ty));
     }
@@ -403,19 +403,14 @@ __global__ void __launch_bounds__(256) k_firststep(Geom g, Slots s, Inter in, co
     }
 }
 
-void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const StepParams *p, bool decide, bool mixed) {
+void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const StepParams *p, bool decide, bool) {
     const int b = 256, n = (g.n_local + b - 1) / b;
-    if (mixed) {
-        if (decide) k_firststep<true, true, true><<<n, b, 0, lc.stream>>>(g, s, in, p);
-        else k_firststep<true, false, true><<<n, b, 0, lc.stream>>>(g, s, in, p);
-    } else {
-        if (decide) k_firststep<true, true, false><<<n, b, 0, lc.stream>>>(g, s, in, p);
-        else k_firststep<true, false, false><<<n, b, 0, lc.stream>>>(g, s, in, p);
-    }
+    if (decide) k_firststep<true, true><<<n, b, 0, lc.stream>>>(g, s, in, p);
+    else k_firststep<true, false><<<n, b, 0, lc.stream>>>(g, s, in, p);
 }
 void launch_decide_scan(const LaunchCtx &lc, const Geom &g, Slots s, Inter in) {
     const int b = 256, n = (g.n_local + b - 1) / b;
-    k_firststep<false, true, false><<<n, b, 0, lc.stream>>>(g, s, in, nullptr);
+    k_firststep<false, true><<<n, b, 0, lc.stream>>>(g, s, in, nullptr);
 }
 
 __global__ void k_inter_firststep(Inter in, const StepParams *__restrict__ p) {
@@ -471,7 +466,6 @@ __device__ __forceinline__ int ghost_slot(const Geom &g, int t) {
     return lin(g, X, Y, Z);
 }
 
-template <bool MIXED>
 __global__ void k_ghost_copy(Geom g, Slots s) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= g.n_ghost_slots) return;
@@ -484,12 +478,11 @@ __global__ void k_ghost_copy(Geom g, Slots s) {
     s.x[gs] = sx ? __dadd_rn(ox, sx > 0 ? g.L[0] : -g.L[0]) : ox;
     s.y[gs] = sy ? __dadd_rn(oy, sy > 0 ? g.L[1] : -g.L[1]) : oy;
     s.z[gs] = sz ? __dadd_rn(oz, sz > 0 ? g.L[2] : -g.L[2]) : oz;
-    if (MIXED) s.u4[sidx(g, gs)] = s.u4[sidx(g, os)];
+    s.u4[sidx(g, gs)] = s.u4[sidx(g, os)];
 }
-void launch_ghost_copy(const LaunchCtx &lc, const Geom &g, Slots s, bool mixed) {
+void launch_ghost_copy(const LaunchCtx &lc, const Geom &g, Slots s, bool) {
     const int b = 256, n = (g.n_ghost_slots + b - 1) / b;
-    if (mixed) k_ghost_copy<true><<<n, b, 0, lc.stream>>>(g, s);
-    else k_ghost_copy<false><<<n, b, 0, lc.stream>>>(g, s);
+    k_ghost_copy<<<n, b, 0, lc.stream>>>(g, s);
 }
 
 // forward df (DfEmbedPacker, src/pack/df_embed_packer.cpp): lattice ghosts and ghost inter atoms
@@ -517,15 +510,29 @@ void launch_ghost_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool
 // Warps are parity-uniform (gather_slot), so the candidate loop reads warp-uniform constants; far
 // atoms continue over the entries beyond the pruned set.
 // ------------------------------------------------------------------------------------------------
+// FP32 candidate test of the FP64 gathers: r^2 from the u4 displacements, against rc^2 (1 + 1e-4).
+// Its error is below 1e-6 of rc^2, so every pair the exact FP64 test accepts passes it; vacancies
+// (NaN) never do. Only candidates that pass load their FP64 positions.
+__device__ __forceinline__ bool near_f32(const Geom &g, f2 uixy, float uiz, float4 D, float4 uj) {
+    const f2 dxy = f2_sub(f2_sub(uixy, f2_pack(uj.x, uj.y)), f2_pack(D.x, D.y));
+    const float dz = (uiz - uj.z) - D.z;
+    float dx, dy;
+    f2_unpack(dxy, dx, dy);
+    return dx * dx + dy * dy + dz * dz < g.rc2_pre;
+}
+
 template <int PAR>
 __device__ __forceinline__ double rho_sum_fp64(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int sl,
-                                               double xi, double yi, double zi, int q0, int q1) {
+                                               int si, float4 ui, double xi, double yi, double zi, int q0, int q1) {
     double acc = 0.0;
+    const f2 uixy = f2_pack(ui.x, ui.y);
 #pragma unroll 4
     for (int q = q0; q < q1; q++) {
+        const float4 D = nt.cand[PAR][q];
+        const float4 uj = __ldg(s.u4 + si + __float_as_int(D.w));
+        if (!near_f32(g, uixy, ui.z, D, uj)) continue;
         const int sj = sl + nt.lat[PAR][q];
-        const int tj = s.type[sj];
-        if (tj < 0) continue;
+        const int tj = __float_as_int(uj.w);
         const double dx = xi - s.x[sj], dy = yi - s.y[sj], dz = zi - s.z[sj];
         const double r2 = dx * dx + dy * dy + dz * dz;
         if (r2 < g.rc2) {
@@ -546,11 +553,15 @@ __global__ void __launch_bounds__(512) k_lat_rho_fp64(const __grid_constant__ Ne
     const int ti = s.type[sl];
     if (ti < 0) { s.rho[sl] = 0.0; return; }
     const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
+    const int si = sidx(g, sl);
+    const float4 ui = s.u4[si];
     const int np = nt.npruned;
-    double acc = par ? rho_sum_fp64<1>(nt, g, s, pt, sl, xi, yi, zi, 0, np) : rho_sum_fp64<0>(nt, g, s, pt, sl, xi, yi, zi, 0, np);
+    double acc = par ? rho_sum_fp64<1>(nt, g, s, pt, sl, si, ui, xi, yi, zi, 0, np)
+                     : rho_sum_fp64<0>(nt, g, s, pt, sl, si, ui, xi, yi, zi, 0, np);
     if (in.far_flag[sl]) {
         const int nf = nt.nfull;
-        acc += par ? rho_sum_fp64<1>(nt, g, s, pt, sl, xi, yi, zi, np, nf) : rho_sum_fp64<0>(nt, g, s, pt, sl, xi, yi, zi, np, nf);
+        acc += par ? rho_sum_fp64<1>(nt, g, s, pt, sl, si, ui, xi, yi, zi, np, nf)
+                   : rho_sum_fp64<0>(nt, g, s, pt, sl, si, ui, xi, yi, zi, np, nf);
     }
     s.rho[sl] = acc;
     if (!hook && lattice_only(in)) {
@@ -653,14 +664,17 @@ void launch_lat_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTab
 // ------------------------------------------------------------------------------------------------
 template <int PAR>
 __device__ __forceinline__ void force_sum_fp64(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int sl, int ti,
-                                               double xi, double yi, double zi, double dfi, int q0, int q1,
+                                               int si, float4 ui, double xi, double yi, double zi, double dfi, int q0, int q1,
                                                double &fx, double &fy, double &fz) {
     const Knot64 *rho_di = pt.rho_d + ti * pt.nr;
+    const f2 uixy = f2_pack(ui.x, ui.y);
 #pragma unroll 2
     for (int q = q0; q < q1; q++) {
+        const float4 D = nt.cand[PAR][q];
+        const float4 uj = __ldg(s.u4 + si + __float_as_int(D.w));
+        if (!near_f32(g, uixy, ui.z, D, uj)) continue;
         const int sj = sl + nt.lat[PAR][q];
-        const int tj = s.type[sj];
-        if (tj < 0) continue;
+        const int tj = __float_as_int(uj.w);
         const double dx = xi - s.x[sj], dy = yi - s.y[sj], dz = zi - s.z[sj];
         const double r2 = dx * dx + dy * dy + dz * dz;
         if (r2 < g.rc2) {
@@ -694,14 +708,16 @@ __global__ void __launch_bounds__(512) k_lat_force_fp64(const __grid_constant__ 
     if (ti < 0) { s.fx[sl] = 0.0; s.fy[sl] = 0.0; s.fz[sl] = 0.0; return; }
     const double xi = s.x[sl], yi = s.y[sl], zi = s.z[sl];
     const double dfi = s.df[sl];
+    const int si = sidx(g, sl);
+    const float4 ui = s.u4[si];
     double fx = 0.0, fy = 0.0, fz = 0.0;
     const int np = nt.npruned;
-    if (par) force_sum_fp64<1>(nt, g, s, pt, sl, ti, xi, yi, zi, dfi, 0, np, fx, fy, fz);
-    else force_sum_fp64<0>(nt, g, s, pt, sl, ti, xi, yi, zi, dfi, 0, np, fx, fy, fz);
+    if (par) force_sum_fp64<1>(nt, g, s, pt, sl, ti, si, ui, xi, yi, zi, dfi, 0, np, fx, fy, fz);
+    else force_sum_fp64<0>(nt, g, s, pt, sl, ti, si, ui, xi, yi, zi, dfi, 0, np, fx, fy, fz);
     if (in.far_flag[sl]) {
         const int nf = nt.nfull;
-        if (par) force_sum_fp64<1>(nt, g, s, pt, sl, ti, xi, yi, zi, dfi, np, nf, fx, fy, fz);
-        else force_sum_fp64<0>(nt, g, s, pt, sl, ti, xi, yi, zi, dfi, np, nf, fx, fy, fz);
+        if (par) force_sum_fp64<1>(nt, g, s, pt, sl, ti, si, ui, xi, yi, zi, dfi, np, nf, fx, fy, fz);
+        else force_sum_fp64<0>(nt, g, s, pt, sl, ti, si, ui, xi, yi, zi, dfi, np, nf, fx, fy, fz);
     }
     s.fx[sl] = fx; s.fy[sl] = fy; s.fz[sl] = fz;
     if (kick && !hook && lattice_only(in)) {
@@ -890,6 +906,14 @@ __global__ void __launch_bounds__(kVmaxSlots) k_step_head(StepParams *p) {
     p->steps = k + 1;
 }
 void launch_step_head(const LaunchCtx &lc, StepParams *sp) { k_step_head<<<1, kVmaxSlots, 0, lc.stream>>>(sp); }
+// steps taken and simulated time into a sample record (stage machine thermo output)
+__global__ void k_clock_sample(const StepParams *p, double *out) {
+    out[0] = (double) p->steps;
+    out[1] = p->time;
+}
+void launch_clock_sample(const LaunchCtx &lc, const StepParams *sp, double *out) {
+    k_clock_sample<<<1, 1, 0, lc.stream>>>(sp, out);
+}
 // max |v|^2 over local lattice atoms and local inter atoms, from scratch
 __global__ void k_vmax_full(Geom g, Slots s, Inter in, StepParams *p) {
     const int stride = gridDim.x * blockDim.x;
@@ -1135,7 +1159,7 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
                 in.df[a] = mixed ? (double) s.df32[sidx(g, sl)] : s.df[sl];
                 s.type[sl] = kInvalid;
                 s.vx[sl] = 0.0; s.vy[sl] = 0.0; s.vz[sl] = 0.0;
-                if (mixed) s.u4[sidx(g, sl)] = vacant_u4();
+                s.u4[sidx(g, sl)] = vacant_u4();
             }
             __syncthreads();
             if (tid == 0) in.cnt[CNT_INTER] = n0 + nd;
@@ -1167,7 +1191,7 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
             s.type[sl] = (int8_t) in.type[a];
             s.x[sl] = in.x[a]; s.y[sl] = in.y[a]; s.z[sl] = in.z[a];
             s.vx[sl] = in.vx[a]; s.vy[sl] = in.vy[a]; s.vz[sl] = in.vz[a];
-            if (mixed) {
+            {
                 const int X = sl % g.Sx, r = sl / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
                 double xs, ys, zs;
                 site_of(g, X, Y, Z, xs, ys, zs);

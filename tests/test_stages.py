@@ -1,0 +1,69 @@
+"""The stage machine (mg_run_stages) against the reference's driver logic (MDSimulation::beforeStep /
+postStep, frontend/md_simulation.cpp:40-111) restated here on the oracle's step primitives."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+A0 = 2.855
+RCF = 5.6 / A0
+
+
+def run_stages_oracle(ref, stages, steps, default_dt, n_atoms, thermo_interval):
+    cur, cur_steps, stage_len, nxt, samples = None, 0, 0, 0, []
+    for step in range(steps):
+        if cur_steps >= stage_len:
+            cur = stages[nxt]
+            nxt += 1
+            stage_len = cur["steps"]
+            cur_steps = 0
+            ref.set_timestep(cur.get("step_length", 0.0) or default_dt)
+        if "collision_step" in cur and cur_steps + 1 == cur["collision_step"]:
+            ref.collision_step(cur["lat"], cur["direction"], cur["energy"])
+        if "rescale_t" in cur and cur_steps % cur["rescale_every"] == 0:
+            ref.rescale(cur["rescale_t"], n_atoms)
+        ref.simulate(1)
+        cur_steps += 1
+        if thermo_interval and (step + 1) % thermo_interval == 0:
+            samples.append((ref.mvv(), ref.time()))
+    return samples
+
+
+def test_stage_machine_matches_the_reference_driver(pkg, orc, wl, potentials, gpu_lib):
+    cells = (9, 9, 9)
+    n = 2 * 9 * 9 * 9
+    atoms = wl.build_state(cells, A0, RCF, temperature=300.0, seed=121)
+    stages = [
+        {"steps": 20, "step_length": 0.0005, "rescale_t": 600.0, "rescale_every": 5},
+        {"steps": 15, "collision_step": 3, "lat": [4, 4, 4, 1], "direction": [1.0, 2.0, 2.5], "energy": 150.0},
+        {"steps": 12, "step_length": 0.0002},
+        {"steps": 0, "step_length": 0.0003},          # a stage of 0 steps still runs one step
+        {"steps": 5},
+    ]
+    steps = 20 + 15 + 12 + 1 + 5
+    ctx = pkg.Context(cells, A0, RCF, precision="fp64")
+    ctx.pot_init_setfl(potentials["fe"])
+    ctx.upload(atoms)
+    ctx.prepare()
+    got = ctx.run_stages(stages, steps, default_dt=0.001, n_atoms=n, thermo_interval=4)
+    ref = orc.OracleSim(cells, A0, RCF, potentials["fe"], dt=0.001)
+    ref.set_atoms(atoms)
+    ref.prepare()
+    want = run_stages_oracle(ref, stages, steps, 0.001, n, 4)
+    assert len(got) == len(want) == steps // 4
+    for k, (g, (mvv, t)) in enumerate(zip(got, want)):
+        assert g["step"] == 4 * (k + 1)
+        assert g["time_ps"] == t                       # the same dt sequence, summed in the same order
+        assert g["mvv"] == pytest.approx(mvv, rel=1e-10)
+    a, inter = ctx.download()
+    loc = wl.local_slot_indices(cells, RCF)
+    w = ref.get_atoms()
+    assert np.abs(a["x"][loc] - w["x"][loc]).max() < 1e-9
+    assert np.array_equal(inter["id"], ref.get_inter()["id"])
+    hist = ctx.dt_history()
+    assert np.array_equal(hist[:20], [0.0005] * 20) and np.array_equal(hist[35:47], [0.0002] * 12)
+    assert hist[47] == 0.0003 and np.array_equal(hist[48:], [0.001] * 5)
+    with pytest.raises(pkg.MgError) as e:
+        ctx.run_stages([{"steps": 2}], 5, default_dt=0.001, n_atoms=n)   # runs out of stages
+    assert e.value.status == 6
+    ctx.close()
