@@ -548,7 +548,9 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 pair/spline terms, compensated f32 sums, f64 state", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f32",
+        "dtype_detail": "f32 distances, spline lookups and pair terms; Kahan-compensated f32 sums; f64 positions, "
+                        "velocities, Verlet and reductions", "data": "synthetic",
         "config": {"workload": f"{w.name}: BCC Fe-1.5at%Cu-1.0at%Ni, {w.cells[0]}^3 unit cells = {n_atoms} atoms, "
                                f"{w.temperature:.0f} K Maxwell start, dt {w.dt * 1000:.0f} fs, synthetic 3-element setfl "
                                f"(nr = nrho = 5000, rc 5.6 A)",

@@ -158,8 +158,14 @@ void seq_firststep(mg_context *ctx, bool decide, Timer *t) {
 void seq_compute_eam(mg_context *ctx, bool kick, bool with_manage_prefix, int manage_mask, Timer *t) {
     const LaunchCtx lc = ctx->lc();
     const bool mx = ctx->mixed();
+    const bool decide = with_manage_prefix && (manage_mask & MANAGE_DECIDE);
+    if (decide) {
+        launch_displaced_collect(lc, ctx->g, ctx->in);  // the displaced slots of firststep, in scan order
+        launch_far_clear(lc, ctx->g, ctx->in);           // the previous far list's neighbourhood marks
+    }
     if (with_manage_prefix) launch_inter_manage(lc, ctx->g, ctx->s, ctx->in, manage_mask | MANAGE_INDEX, mx);
     else launch_inter_manage(lc, ctx->g, ctx->s, ctx->in, MANAGE_INDEX, mx);
+    if (decide) launch_far_mark(lc, ctx->g, ctx->in);   // the new far list's neighbourhoods
     if (t) t->mark(3);
     launch_ghost_copy(lc, ctx->g, ctx->s, mx);
     if (t) t->mark(4);
@@ -185,7 +191,7 @@ void seq_step(mg_context *ctx, Timer *t) {
     seq_firststep(ctx, true, t);
     seq_compute_eam(ctx, true, true, MANAGE_DECIDE | MANAGE_CLEAR_GHOST | MANAGE_EXCHANGE | MANAGE_BORDER, t);
 }
-constexpr int kLaunchesPerStep = 12;
+constexpr int kLaunchesPerStep = 17;
 
 mg_status require_ready(mg_context *ctx) {
     if (!ctx->pot_ready) { ctx->err = "potential not initialised"; return MG_ERR_POTENTIAL; }
@@ -477,6 +483,11 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     ALLOC(in.gx, gcap); ALLOC(in.gy, gcap); ALLOC(in.gz, gcap); ALLOC(in.gdf, gcap);
     ALLOC(in.scratch_i, 3 * cap); ALLOC(in.scratch_d, 13 * cap); ALLOC(in.scratch_u, cap);
     ALLOC(in.displaced, (size_t) in.dcap);
+    {
+        const size_t nblocks = (static_cast<size_t>(g.n_local) + kFirstThreads - 1) / kFirstThreads;
+        ALLOC(in.dmask, nblocks * (kFirstThreads / 32));
+        ALLOC(in.dblock, nblocks);
+    }
     ALLOC(in.claim, ns);
     ALLOC(in.far_list, (size_t) in.fcap);
     ALLOC(in.far_flag, ns);
@@ -857,7 +868,10 @@ mg_status mg_phase(mg_context *ctx, int32_t phase) {
         case 0: seq_firststep(ctx, false, nullptr); break;
         case 1:
             launch_decide_scan(lc, ctx->g, ctx->s, ctx->in);
+            launch_displaced_collect(lc, ctx->g, ctx->in);
+            launch_far_clear(lc, ctx->g, ctx->in);
             launch_inter_manage(lc, ctx->g, ctx->s, ctx->in, MANAGE_DECIDE | MANAGE_CLEAR_GHOST, ctx->mixed());
+            launch_far_mark(lc, ctx->g, ctx->in);
             break;
         case 2: launch_inter_manage(lc, ctx->g, ctx->s, ctx->in, MANAGE_EXCHANGE, ctx->mixed()); break;
         case 3: launch_inter_manage(lc, ctx->g, ctx->s, ctx->in, MANAGE_BORDER, ctx->mixed()); break;

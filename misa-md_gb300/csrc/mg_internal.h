@@ -16,7 +16,9 @@ constexpr double kBoltz = 8.617343e-5;       // src/types/pre_define.h:11
 constexpr double kMvv2e = 1.0364269e-4;      // src/types/pre_define.h:18
 constexpr double kFtm2v = (1.0 / kMvv2e);    // src/types/pre_define.h:19
 constexpr double kNeiLatCutoff = 0.5;        // src/md_building_config.h.in:24
-constexpr int kMaxFull = 232;                // capacity of a full offset table per parity
+constexpr int kMaxFull = 232;
+constexpr int kFirstThreads = 256;           // firststep block: its displaced ballots and counts
+constexpr int kSortSmemKeys = 16384;         // bucket keys the list manager sorts in shared memory                // capacity of a full offset table per parity
 
 // box flags (src/lattice/box.h:12-20)
 constexpr uint32_t kInBox = 0, kXLow = 1u, kXHigh = 2u, kYLow = 4u, kYHigh = 8u, kZLow = 16u, kZHigh = 32u;
@@ -96,9 +98,11 @@ struct Inter {
     int *scratch_i;          // 2 * (cap + gcap)
     double *scratch_d;       // 13 * cap
     uint64_t *scratch_u;     // cap
-    // displaced lattice slots found by the decide scan (unordered)
+    // displaced lattice slots found by the decide scan, in scan order
     int *displaced;
     int dcap;
+    unsigned *dmask;         // per firststep warp: ballot of displaced slots
+    int *dblock;             // per firststep block: displaced count, then its exclusive offset
     // per-slot claim word for recombination (INT_MAX when free)
     int *claim;
     // lattice atoms farther than 0.2 a0 from their site (only recombined atoms after decide): they
@@ -218,6 +222,11 @@ void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, con
 // fill g.site_half (once per context)
 void launch_site_table(const LaunchCtx &lc, const Geom &g, double *site_half);
 void launch_decide_scan(const LaunchCtx &lc, const Geom &g, Slots s, Inter in);
+// after a deciding firststep: the displaced slots in scan order into in.displaced, count in CNT_DISPLACED
+void launch_displaced_collect(const LaunchCtx &lc, const Geom &g, Inter in);
+// far-atom neighbourhood marks: clear those of the current far list / set them (grid-wide)
+void launch_far_clear(const LaunchCtx &lc, const Geom &g, Inter in);
+void launch_far_mark(const LaunchCtx &lc, const Geom &g, Inter in);
 void launch_ghost_copy(const LaunchCtx &lc, const Geom &g, Slots s, bool mixed);
 void launch_ghost_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool mixed);
 void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook);

@@ -23,7 +23,9 @@ namespace mg {
 // ------------------------------------------------------------------------------------------------
 __constant__ double c_mass[3];
 
+void configure_manage_kernel();
 void set_mass_table(cudaStream_t stream) {
+    configure_manage_kernel();
     const double mass[3] = {atom_mass(0), atom_mass(1), atom_mass(2)};
     cudaMemcpyToSymbolAsync(c_mass, mass, sizeof(mass), 0, cudaMemcpyHostToDevice, stream);
     cudaStreamSynchronize(stream);
@@ -358,59 +360,143 @@ void launch_site_table(const LaunchCtx &lc, const Geom &g, double *site_half) {
     k_site_table<<<(g.n_site_half + 255) / 256, 256, 0, lc.stream>>>(g.a0, g.n_site_half, site_half);
 }
 
+// Displaced slots are recorded in scan order without a sort: each warp writes the ballot of its 32
+// slots (thread t holds local slot t in k, j, i order). A grid kernel sums the ballots of each group of
+// kFirstThreads / 32 warps, a one-block scan turns the sums into offsets, and a collect kernel writes
+// the slots in order. The firststep itself has no block barrier.
 template <bool MOVE, bool DECIDE>
-__global__ void __launch_bounds__(256) k_firststep(Geom g, Slots s, Inter in, const StepParams *__restrict__ p) {
+__global__ void __launch_bounds__(kFirstThreads) k_firststep(Geom g, Slots s, Inter in, const StepParams *__restrict__ p) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.n_local) return;
-    int i, j, k;
-    const int sl = local_slot(g, t, i, j, k);
-    const int ty = s.type[sl];
-    if (ty < 0) return;
-    double x = s.x[sl], y = s.y[sl], z = s.z[sl];
-    if (MOVE) {
-        const double c = dt_inv_m_of(p, ty);
-        double vx = s.vx[sl], vy = s.vy[sl], vz = s.vz[sl];
-        vx = __dadd_rn(vx, __dmul_rn(c, s.fx[sl]));
-        vy = __dadd_rn(vy, __dmul_rn(c, s.fy[sl]));
-        vz = __dadd_rn(vz, __dmul_rn(c, s.fz[sl]));
-        const double dt = p->dt;
-        x = __dadd_rn(x, __dmul_rn(dt, vx));
-        y = __dadd_rn(y, __dmul_rn(dt, vy));
-        z = __dadd_rn(z, __dmul_rn(dt, vz));
-        s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz;
-        s.x[sl] = x; s.y[sl] = y; s.z[sl] = z;
+    bool disp = false;
+    int ty = -1, sl = 0, i = 0, j = 0, k = 0;
+    if (t < g.n_local) {
+        sl = local_slot(g, t, i, j, k);
+        ty = s.type[sl];
     }
-    // the site from the table (the same rounded values site_of computes; gx is even, so the x parity
-    // of the slot is i & 1)
-    const int par = i & 1;
-    const double xs = g.site_half[i], ys = g.site_half[2 * j + par], zs = g.site_half[2 * k + par];
-    const double ex = __dsub_rn(x, xs), ey = __dsub_rn(y, ys), ez = __dsub_rn(z, zs);
-    const float exf = __double2float_rn(ex), eyf = __double2float_rn(ey), ezf = __double2float_rn(ez);
-    if (MOVE) {
-        const float ih = g.inv_h_f;
-        s.u4[sidx(g, sl)] = make_float4(exf * ih, eyf * ih, ezf * ih, __int_as_float(ty));
-    }
-    // the exact FP64 test of decide runs only where the FP32 distance is not clearly below it
-    if (DECIDE && !(exf * exf + eyf * eyf + ezf * ezf < g.thr_lo_f)) {
-        double dist = __dmul_rn(ex, ex);
-        dist = __dadd_rn(dist, __dmul_rn(ey, ey));
-        dist = __dadd_rn(dist, __dmul_rn(ez, ez));
-        if (dist > g.thr) {
-            const int q = atomicAdd(&in.cnt[CNT_DISPLACED], 1);
-            if (q < in.dcap) in.displaced[q] = sl;
-            else set_error(in, MG_DEVERR_DISPLACED_OVERFLOW);
+    if (ty >= 0) {
+        double x = s.x[sl], y = s.y[sl], z = s.z[sl];
+        if (MOVE) {
+            const double c = dt_inv_m_of(p, ty);
+            double vx = s.vx[sl], vy = s.vy[sl], vz = s.vz[sl];
+            vx = __dadd_rn(vx, __dmul_rn(c, s.fx[sl]));
+            vy = __dadd_rn(vy, __dmul_rn(c, s.fy[sl]));
+            vz = __dadd_rn(vz, __dmul_rn(c, s.fz[sl]));
+            const double dt = p->dt;
+            x = __dadd_rn(x, __dmul_rn(dt, vx));
+            y = __dadd_rn(y, __dmul_rn(dt, vy));
+            z = __dadd_rn(z, __dmul_rn(dt, vz));
+            s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz;
+            s.x[sl] = x; s.y[sl] = y; s.z[sl] = z;
         }
+        // the site from the table (the same rounded values site_of computes; gx is even, so the x
+        // parity of the slot is i & 1)
+        const int par = i & 1;
+        const double xs = g.site_half[i], ys = g.site_half[2 * j + par], zs = g.site_half[2 * k + par];
+        const double ex = __dsub_rn(x, xs), ey = __dsub_rn(y, ys), ez = __dsub_rn(z, zs);
+        const float exf = __double2float_rn(ex), eyf = __double2float_rn(ey), ezf = __double2float_rn(ez);
+        if (MOVE) {
+            const float ih = g.inv_h_f;
+            s.u4[sidx(g, sl)] = make_float4(exf * ih, eyf * ih, ezf * ih, __int_as_float(ty));
+        }
+        // the exact FP64 test of decide runs only where the FP32 distance is not clearly below it
+        if (DECIDE && !(exf * exf + eyf * eyf + ezf * ezf < g.thr_lo_f)) {
+            double dist = __dmul_rn(ex, ex);
+            dist = __dadd_rn(dist, __dmul_rn(ey, ey));
+            dist = __dadd_rn(dist, __dmul_rn(ez, ez));
+            disp = dist > g.thr;
+        }
+    }
+    if (DECIDE) {
+        const unsigned m = __ballot_sync(0xffffffffu, disp);
+        if ((threadIdx.x & 31) == 0) in.dmask[t >> 5] = m;
+    }
+}
+
+// displaced count of each group of kFirstThreads / 32 ballots
+__global__ void k_disp_count(Inter in, int nblocks) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nblocks) return;
+    constexpr int kWarps = kFirstThreads / 32;
+    int c = 0;
+    for (int w = 0; w < kWarps; w++) c += __popc(in.dmask[b * kWarps + w]);
+    in.dblock[b] = c;
+}
+
+// one block: block counts -> exclusive offsets (in place), total -> CNT_DISPLACED (clamped to dcap)
+__global__ void __launch_bounds__(1024) k_disp_scan(Inter in, int nblocks) {
+    __shared__ int warp_tot[32];
+    __shared__ int running;
+    if (threadIdx.x == 0) running = 0;
+    __syncthreads();
+    for (int c0 = 0; c0 < nblocks; c0 += blockDim.x) {
+        const int b = c0 + threadIdx.x;
+        const int v = b < nblocks ? in.dblock[b] : 0;
+        int x = v;  // inclusive warp scan
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if ((threadIdx.x & 31) >= o) x += y;
+        }
+        if ((threadIdx.x & 31) == 31) warp_tot[threadIdx.x >> 5] = x;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            int w = threadIdx.x < (blockDim.x >> 5) ? warp_tot[threadIdx.x] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, w, o);
+                if (threadIdx.x >= o) w += y;
+            }
+            warp_tot[threadIdx.x] = w;  // inclusive over warps
+        }
+        __syncthreads();
+        const int warp_base = (threadIdx.x >> 5) ? warp_tot[(threadIdx.x >> 5) - 1] : 0;
+        const int base = running;
+        if (b < nblocks) in.dblock[b] = base + warp_base + x - v;
+        __syncthreads();
+        if (threadIdx.x == 0) running = base + warp_tot[(blockDim.x >> 5) - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        int total = running;
+        if (total > in.dcap) { set_error(in, MG_DEVERR_DISPLACED_OVERFLOW); total = in.dcap; }
+        in.cnt[CNT_DISPLACED] = total;
+    }
+}
+
+// one thread per warp mask: the displaced slots of those 32 threads, in order, at their offsets
+__global__ void k_disp_collect(Geom g, Inter in, int nwarps) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (in.cnt[CNT_DISPLACED] == 0 || w >= nwarps) return;
+    unsigned m = in.dmask[w];
+    if (m == 0) return;
+    constexpr int kWarpsPerBlock = kFirstThreads / 32;
+    const int b = w / kWarpsPerBlock;
+    int rank = in.dblock[b];
+    for (int v = b * kWarpsPerBlock; v < w; v++) rank += __popc(in.dmask[v]);
+    while (m) {
+        const int bit = __ffs(m) - 1;
+        m &= m - 1;
+        if (rank < in.dcap) {
+            int i, j, k;
+            in.displaced[rank] = local_slot(g, (w << 5) + bit, i, j, k);
+        }
+        rank++;
     }
 }
 
 void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const StepParams *p, bool decide, bool) {
-    const int b = 256, n = (g.n_local + b - 1) / b;
+    const int b = kFirstThreads, n = (g.n_local + b - 1) / b;
     if (decide) k_firststep<true, true><<<n, b, 0, lc.stream>>>(g, s, in, p);
     else k_firststep<true, false><<<n, b, 0, lc.stream>>>(g, s, in, p);
 }
 void launch_decide_scan(const LaunchCtx &lc, const Geom &g, Slots s, Inter in) {
-    const int b = 256, n = (g.n_local + b - 1) / b;
+    const int b = kFirstThreads, n = (g.n_local + b - 1) / b;
     k_firststep<false, true><<<n, b, 0, lc.stream>>>(g, s, in, nullptr);
+}
+void launch_displaced_collect(const LaunchCtx &lc, const Geom &g, Inter in) {
+    const int nblocks = (g.n_local + kFirstThreads - 1) / kFirstThreads;
+    const int nwarps = nblocks * (kFirstThreads / 32);
+    k_disp_count<<<(nblocks + 255) / 256, 256, 0, lc.stream>>>(in, nblocks);
+    k_disp_scan<<<1, 1024, 0, lc.stream>>>(in, nblocks);
+    k_disp_collect<<<(nwarps + 255) / 256, 256, 0, lc.stream>>>(g, in, nwarps);
 }
 
 __global__ void k_inter_firststep(Inter in, const StepParams *__restrict__ p) {
@@ -576,6 +662,7 @@ __device__ __forceinline__ void rho_sum_mixed(const NeighTables &nt, const Geom 
                                               int q0, int q1, float &sum, float &comp) {
     const float rc2 = g.rc2_h;
     const float hinv = pt.h_inv_dr_f;
+    const int nr = pt.nr;
     const f2 uixy = f2_pack(ui.x, ui.y);
 #pragma unroll 4
     for (int q = q0; q < q1; q++) {
@@ -590,8 +677,8 @@ __device__ __forceinline__ void rho_sum_mixed(const NeighTables &nt, const Geom 
             const int tj = __float_as_int(uj.w);
             const float rp = r2 * rsqrtf(r2);
             int m; float p;
-            locate_r_f(rp, hinv, pt.nr, m, p);
-            kahan(sum, comp, val_f(pt.rho_vf + tj * pt.nr, m, p));
+            locate_r_f(rp, hinv, nr, m, p);
+            kahan(sum, comp, val_f(pt.rho_vf + tj * nr, m, p));
         }
     }
 }
@@ -733,12 +820,8 @@ __global__ void __launch_bounds__(512) k_lat_force_fp64(const __grid_constant__ 
 template <int PAR>
 __device__ __forceinline__ void force_sum_mixed(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int si, int ti,
                                                 float4 ui, float dfi, int q0, int q1, f2 &sxy, f2 &cxy, float &sz, float &cz) {
-    const float rc2 = g.rc2_h;
-    const float hinv = pt.h_inv_dr_f;
-    const float inv_h = 1.0f / g.h_f;
-    const float inv_dr = pt.inv_dr_f;
-    const float4 *rho_di = pt.rho_dff + ti * pt.nr;
-    const float *zr_i = pt.zr8 + 8 * (ti * 3) * pt.nr;
+    // records of the pair row ti; the table constants are read from the parameter bank where used
+    const int fbase = (ti * 3) * pt.nr;
     const f2 uixy = f2_pack(ui.x, ui.y);
 #pragma unroll 2
     for (int q = q0; q < q1; q++) {
@@ -750,24 +833,24 @@ __device__ __forceinline__ void force_sum_mixed(const NeighTables &nt, const Geo
         float dx, dy;
         f2_unpack(dxy, dx, dy);
         const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 < rc2) {  // false for vacancies (NaN coordinates)
+        if (r2 < g.rc2_h) {  // false for vacancies (NaN coordinates)
             const int tj = __float_as_int(uj.w);
             const float rinv_h = rsqrtf(r2);
             const float rp = r2 * rinv_h;
             int m; float p;
-            locate_r_f(rp, hinv, pt.nr, m, p);
+            locate_r_f(rp, pt.h_inv_dr_f, pt.nr, m, p);
             // record {c0, d0, c1, d1, c2, d2, c3, 0}: r*phi = c(p), rho_tj' = d(p), both in one Horner
             float z[8];
-            ld_nc_v8(zr_i + 8 * (tj * pt.nr + m), z);
+            ld_nc_v8(pt.zr8 + 8 * (fbase + tj * pt.nr + m), z);
             const f2 pp = f2_pack(p, p);
             f2 h = f2_fma(f2_pack(z[6], z[7]), pp, f2_pack(z[4], z[5]));
             h = f2_fma(h, pp, f2_pack(z[2], z[3]));
             h = f2_fma(h, pp, f2_pack(z[0], z[1]));
             float zv, rhojp;
             f2_unpack(h, zv, rhojp);
-            const float zp = fmaf(fmaf(3.0f * z[6], p, z[4] + z[4]), p, z[2]) * inv_dr;
-            const float rhoip = (tj == ti) ? rhojp : der_f(rho_di, m, p);
-            const float rinv = rinv_h * inv_h;
+            const float zp = fmaf(fmaf(3.0f * z[6], p, z[4] + z[4]), p, z[2]) * pt.inv_dr_f;
+            const float rhoip = (tj == ti) ? rhojp : der_f(pt.rho_dff + ti * pt.nr, m, p);
+            const float rinv = rinv_h * g.inv_h_f;
             const float phi = zv * rinv;
             const float phip = (zp - phi) * rinv;
             const float psip = dfi * rhojp + __ldg(s.df32 + oj) * rhoip + phip;
@@ -1090,6 +1173,29 @@ __device__ void block_bitonic_sort(long long *buf, int n) {
     }
 }
 
+// the same sort in shared memory (sm holds at least next_pow2(n) keys)
+__device__ void block_bitonic_sort_smem(long long *buf, int n, long long *sm) {
+    int P = 1;
+    while (P < n) P <<= 1;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) sm[i] = i < n ? buf[i] : LLONG_MAX;
+    __syncthreads();
+    for (int kk = 2; kk <= P; kk <<= 1) {
+        for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+            for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                const int l = i ^ jj;
+                if (l > i) {
+                    const long long a = sm[i], b = sm[l];
+                    const bool up = (i & kk) == 0;
+                    if ((a > b) == up) { sm[i] = b; sm[l] = a; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) buf[i] = sm[i];
+    __syncthreads();
+}
+
 // inter record move helpers (scratch layout: 13 doubles per record)
 __device__ __forceinline__ void inter_save(const Inter &in, int a, int dst) {
     double *d = in.scratch_d + 13 * dst;
@@ -1128,27 +1234,18 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
     }
 
     if (mask & MANAGE_DECIDE) {
-        // the far list of the previous step is void: every lattice atom is re-tested below
-        {
-            const int nf = min(in.cnt[CNT_FAR], in.fcap);
-            mark_far_neighbourhoods(nt, g, in, 0, nf, 0, tid, nthr);
-            __syncthreads();
-            if (tid == 0) in.cnt[CNT_FAR] = 0;
-            __syncthreads();
-        }
-        // (i) displaced lattice atoms join the list in scan order
+        // the far list of the previous step is void (its marks were cleared before this kernel)
+        if (tid == 0) in.cnt[CNT_FAR] = 0;
+        __syncthreads();
+        // (i) displaced lattice atoms join the list in scan order (the collected list is ordered)
         int nd = in.cnt[CNT_DISPLACED];
         if (nd > in.dcap) nd = in.dcap;
         const int n0 = in.cnt[CNT_INTER];
         if (nd > 0) {
-            long long *keys = in.bucket;  // reused as sort buffer
-            for (int q = tid; q < nd; q += nthr) keys[q] = in.displaced[q];
-            __syncthreads();
-            block_bitonic_sort(keys, nd);
             int room = in.cap - n0;
             if (nd > room) { if (tid == 0) set_error(in, MG_DEVERR_INTER_OVERFLOW); nd = room; }
             for (int q = tid; q < nd; q += nthr) {
-                const int sl = (int) keys[q];
+                const int sl = in.displaced[q];
                 const int a = n0 + q;
                 in.id[a] = s.id[sl];
                 in.type[a] = s.type[sl];
@@ -1204,8 +1301,6 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
                 else set_error(in, MG_DEVERR_DISPLACED_OVERFLOW);
             }
         }
-        __syncthreads();
-        mark_far_neighbourhoods(nt, g, in, 0, min(in.cnt[CNT_FAR], in.fcap), 1, tid, nthr);
         __syncthreads();
         // stable compaction of the survivors
         int base = 0;
@@ -1333,13 +1428,20 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
             in.bucket[e] = (key << 32) | (long long) ref;
         }
         __syncthreads();
-        block_bitonic_sort(in.bucket, total);
+        extern __shared__ long long sm_keys[];
+        if (total <= kSortSmemKeys) block_bitonic_sort_smem(in.bucket, total, sm_keys);
+        else block_bitonic_sort(in.bucket, total);
         if (tid == 0) *in.n_bucket = total;
     }
 }
 
+// the list manager sorts up to kSortSmemKeys bucket keys in dynamic shared memory
+void configure_manage_kernel() {
+    cudaFuncSetAttribute(k_inter_manage, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(kSortSmemKeys * sizeof(long long)));
+}
 void launch_inter_manage(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, int mask, bool mixed) {
-    k_inter_manage<<<1, kManageThreads, 0, lc.stream>>>(*lc.nt, g, s, in, mask, mixed);
+    k_inter_manage<<<1, kManageThreads, kSortSmemKeys * sizeof(long long), lc.stream>>>(*lc.nt, g, s, in, mask, mixed);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -1399,11 +1501,21 @@ __device__ __forceinline__ double lat_df(const Geom &g, const Slots &s, int sl, 
 }
 
 // kind: 0 density, 1 force, 2 energy
+// One warp per inter atom (the lists hold a few to thousands of atoms, each with ~460 partner
+// entries): the lanes share the 229 lattice entries and the 229 bucket keys of the atom's nearest
+// site, keep partial sums, and reduce them by shuffles in a fixed order. Shares that belong to
+// lattice atoms go to their owning slots with FP64 atomics, as the reference's Newton-3 scatter.
+__device__ __forceinline__ double warp_sum_d(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
 template <int KIND>
-__global__ void k_inter_eam(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool mixed) {
+__global__ void __launch_bounds__(128) k_inter_eam(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool mixed) {
     const int n = in.cnt[CNT_INTER];
     const int nb = *in.n_bucket;
-    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int a = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); a < n; a += warps) {  // warp-uniform
         const double xa = in.x[a], ya = in.y[a], za = in.z[a];
         const int ta = in.type[a];
         const uint64_t ida = in.id[a];
@@ -1414,7 +1526,7 @@ __global__ void k_inter_eam(const __grid_constant__ NeighTables nt, Geom g, Slot
         // lattice partners: the nearest site's atom, then the full offsets of that site
         const int par = (near % g.Sx) & 1;
         const int nf = nt.nfull;
-        for (int q = -1; q < nf; q++) {
+        for (int q = lane - 1; q < nf; q += 32) {
             const int sj = q < 0 ? near : near + (par ? nt.full[1][q] : nt.full[0][q]);
             if (sj < 0 || sj >= g.n_slots) { set_error(in, MG_DEVERR_OUT_OF_GRID); continue; }
             const int tj = s.type[sj];
@@ -1439,7 +1551,7 @@ __global__ void k_inter_eam(const __grid_constant__ NeighTables nt, Geom g, Slot
             }
         }
         // inter partners: same-site bucket (not itself), then the buckets of the full offsets
-        for (int q = -1; q < nf; q++) {
+        for (int q = lane - 1; q < nf; q += 32) {
             const int key = q < 0 ? near : near + (par ? nt.full[1][q] : nt.full[0][q]);
             for (int b = bucket_begin(in, nb, key); b < nb && (int) (in.bucket[b] >> 32) == key; b++) {
                 const InterRef o = inter_ref(in, (int) (in.bucket[b] & 0xffffffffLL));
@@ -1456,6 +1568,14 @@ __global__ void k_inter_eam(const __grid_constant__ NeighTables nt, Geom g, Slot
                 }
             }
         }
+        if (KIND == 1) {
+            fx = warp_sum_d(fx);
+            fy = warp_sum_d(fy);
+            fz = warp_sum_d(fz);
+        } else {
+            acc = warp_sum_d(acc);
+        }
+        if (lane != 0) continue;
         if (KIND == 0) {
             in.rho[a] = acc;
             int m; double p;
@@ -1471,13 +1591,13 @@ __global__ void k_inter_eam(const __grid_constant__ NeighTables nt, Geom g, Slot
     }
 }
 void launch_inter_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
-    k_inter_eam<0><<<lc.num_sms, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
+    k_inter_eam<0><<<lc.num_sms * 4, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
 }
 void launch_inter_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
-    k_inter_eam<1><<<lc.num_sms, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
+    k_inter_eam<1><<<lc.num_sms * 4, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
 }
 void launch_inter_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
-    k_inter_eam<2><<<lc.num_sms, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
+    k_inter_eam<2><<<lc.num_sms * 4, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -1486,10 +1606,9 @@ void launch_inter_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, 
 // ------------------------------------------------------------------------------------------------
 __global__ void k_far_clear(const __grid_constant__ NeighTables nt, Geom g, Inter in) {
     const int nf = min(in.cnt[CNT_FAR], in.fcap);
-    mark_far_neighbourhoods(nt, g, in, 0, nf, 0, threadIdx.x, blockDim.x);
-    __syncthreads();
-    if (threadIdx.x == 0) in.cnt[CNT_FAR] = 0;
+    mark_far_neighbourhoods(nt, g, in, 0, nf, 0, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
+__global__ void k_far_count_reset(Inter in) { in.cnt[CNT_FAR] = 0; }
 __global__ void k_far_scan(Geom g, Slots s, Inter in) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= g.n_local) return;
@@ -1506,11 +1625,18 @@ __global__ void k_far_mark(const __grid_constant__ NeighTables nt, Geom g, Inter
     const int nf = min(in.cnt[CNT_FAR], in.fcap);
     mark_far_neighbourhoods(nt, g, in, 0, nf, 1, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
+void launch_far_clear(const LaunchCtx &lc, const Geom &g, Inter in) {
+    k_far_clear<<<lc.num_sms * 4, 256, 0, lc.stream>>>(*lc.nt, g, in);
+}
+void launch_far_mark(const LaunchCtx &lc, const Geom &g, Inter in) {
+    k_far_mark<<<lc.num_sms * 4, 256, 0, lc.stream>>>(*lc.nt, g, in);
+}
 void launch_far_rebuild(const LaunchCtx &lc, const Geom &g, Slots s, Inter in) {
-    k_far_clear<<<1, 1024, 0, lc.stream>>>(*lc.nt, g, in);
+    launch_far_clear(lc, g, in);
+    k_far_count_reset<<<1, 1, 0, lc.stream>>>(in);
     const int b = 256;
     k_far_scan<<<(g.n_local + b - 1) / b, b, 0, lc.stream>>>(g, s, in);
-    k_far_mark<<<lc.num_sms, 256, 0, lc.stream>>>(*lc.nt, g, in);
+    launch_far_mark(lc, g, in);
 }
 
 
