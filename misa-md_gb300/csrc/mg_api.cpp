@@ -485,7 +485,7 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     ALLOC(in.displaced, (size_t) in.dcap);
     {
         const size_t nblocks = (static_cast<size_t>(g.n_local) + kFirstThreads - 1) / kFirstThreads;
-        ALLOC(in.dmask, nblocks * (kFirstThreads / 32));
+        ALLOC(in.dflag, nblocks * kFirstThreads);
         ALLOC(in.dblock, nblocks);
     }
     ALLOC(in.claim, ns);
@@ -508,6 +508,9 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     if (e == cudaSuccess) e = cudaMemsetAsync(in.claim, 0x7f, ns * sizeof(int), ctx->stream);  // 0x7f7f7f7f > any list index
     if (e == cudaSuccess) e = cudaMemsetAsync(in.far_flag, 0, ns, ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(in.n_bucket, 0, sizeof(int), ctx->stream);
+    if (e == cudaSuccess)  // the padding past n_local is never written and must read as "not displaced"
+        e = cudaMemsetAsync(in.dflag, 0, ((static_cast<size_t>(g.n_local) + kFirstThreads - 1) / kFirstThreads) * kFirstThreads,
+                            ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s.type, 0xff, ns, ctx->stream);  // all slots INVALID
     if (e == cudaSuccess) e = cudaMemsetAsync(s.u4, 0xff, ns * sizeof(float4), ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_sp, 0, sizeof(StepParams), ctx->stream);

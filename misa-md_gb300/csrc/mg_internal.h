@@ -17,7 +17,7 @@ constexpr double kMvv2e = 1.0364269e-4;      // src/types/pre_define.h:18
 constexpr double kFtm2v = (1.0 / kMvv2e);    // src/types/pre_define.h:19
 constexpr double kNeiLatCutoff = 0.5;        // src/md_building_config.h.in:24
 constexpr int kMaxFull = 232;
-constexpr int kFirstThreads = 256;           // firststep block: its displaced ballots and counts
+constexpr int kFirstThreads = 256;           // firststep block = one group of displaced flags (8 per lane)
 constexpr int kSortSmemKeys = 16384;         // bucket keys the list manager sorts in shared memory                // capacity of a full offset table per parity
 
 // box flags (src/lattice/box.h:12-20)
@@ -101,7 +101,7 @@ struct Inter {
     // displaced lattice slots found by the decide scan, in scan order
     int *displaced;
     int dcap;
-    unsigned *dmask;         // per firststep warp: ballot of displaced slots
+    int8_t *dflag;           // per local slot (k, j, i order, padded to whole firststep blocks): 1 = displaced
     int *dblock;             // per firststep block: displaced count, then its exclusive offset
     // per-slot claim word for recombination (INT_MAX when free)
     int *claim;

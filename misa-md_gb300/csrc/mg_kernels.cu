@@ -360,66 +360,66 @@ void launch_site_table(const LaunchCtx &lc, const Geom &g, double *site_half) {
     k_site_table<<<(g.n_site_half + 255) / 256, 256, 0, lc.stream>>>(g.a0, g.n_site_half, site_half);
 }
 
-// Displaced slots are recorded in scan order without a sort: each warp writes the ballot of its 32
-// slots (thread t holds local slot t in k, j, i order). A grid kernel sums the ballots of each group of
-// kFirstThreads / 32 warps, a one-block scan turns the sums into offsets, and a collect kernel writes
-// the slots in order. The firststep itself has no block barrier.
+// Displaced slots are recorded in scan order without a sort: firststep writes one byte per local slot
+// (thread t holds local slot t in k, j, i order; 1 = displaced). A count kernel sums the bytes of each
+// group of kFirstThreads slots, a one-block scan turns the sums into offsets, and a collect kernel
+// writes the slots in order. firststep keeps its early exits and needs no warp or block collective.
 template <bool MOVE, bool DECIDE>
 __global__ void __launch_bounds__(kFirstThreads) k_firststep(Geom g, Slots s, Inter in, const StepParams *__restrict__ p) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    bool disp = false;
-    int ty = -1, sl = 0, i = 0, j = 0, k = 0;
-    if (t < g.n_local) {
-        sl = local_slot(g, t, i, j, k);
-        ty = s.type[sl];
+    if (t >= g.n_local) return;
+    int i, j, k;
+    const int sl = local_slot(g, t, i, j, k);
+    const int ty = s.type[sl];
+    if (ty < 0) {
+        if (DECIDE) in.dflag[t] = 0;
+        return;
     }
-    if (ty >= 0) {
-        double x = s.x[sl], y = s.y[sl], z = s.z[sl];
-        if (MOVE) {
-            const double c = dt_inv_m_of(p, ty);
-            double vx = s.vx[sl], vy = s.vy[sl], vz = s.vz[sl];
-            vx = __dadd_rn(vx, __dmul_rn(c, s.fx[sl]));
-            vy = __dadd_rn(vy, __dmul_rn(c, s.fy[sl]));
-            vz = __dadd_rn(vz, __dmul_rn(c, s.fz[sl]));
-            const double dt = p->dt;
-            x = __dadd_rn(x, __dmul_rn(dt, vx));
-            y = __dadd_rn(y, __dmul_rn(dt, vy));
-            z = __dadd_rn(z, __dmul_rn(dt, vz));
-            s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz;
-            s.x[sl] = x; s.y[sl] = y; s.z[sl] = z;
-        }
-        // the site from the table (the same rounded values site_of computes; gx is even, so the x
-        // parity of the slot is i & 1)
-        const int par = i & 1;
-        const double xs = g.site_half[i], ys = g.site_half[2 * j + par], zs = g.site_half[2 * k + par];
-        const double ex = __dsub_rn(x, xs), ey = __dsub_rn(y, ys), ez = __dsub_rn(z, zs);
-        const float exf = __double2float_rn(ex), eyf = __double2float_rn(ey), ezf = __double2float_rn(ez);
-        if (MOVE) {
-            const float ih = g.inv_h_f;
-            s.u4[sidx(g, sl)] = make_float4(exf * ih, eyf * ih, ezf * ih, __int_as_float(ty));
-        }
+    double x = s.x[sl], y = s.y[sl], z = s.z[sl];
+    if (MOVE) {
+        const double c = dt_inv_m_of(p, ty);
+        double vx = s.vx[sl], vy = s.vy[sl], vz = s.vz[sl];
+        vx = __dadd_rn(vx, __dmul_rn(c, s.fx[sl]));
+        vy = __dadd_rn(vy, __dmul_rn(c, s.fy[sl]));
+        vz = __dadd_rn(vz, __dmul_rn(c, s.fz[sl]));
+        const double dt = p->dt;
+        x = __dadd_rn(x, __dmul_rn(dt, vx));
+        y = __dadd_rn(y, __dmul_rn(dt, vy));
+        z = __dadd_rn(z, __dmul_rn(dt, vz));
+        s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz;
+        s.x[sl] = x; s.y[sl] = y; s.z[sl] = z;
+    }
+    // the site from the table (the same rounded values site_of computes; gx is even, so the x parity
+    // of the slot is i & 1)
+    const int par = i & 1;
+    const double xs = g.site_half[i], ys = g.site_half[2 * j + par], zs = g.site_half[2 * k + par];
+    const double ex = __dsub_rn(x, xs), ey = __dsub_rn(y, ys), ez = __dsub_rn(z, zs);
+    const float exf = __double2float_rn(ex), eyf = __double2float_rn(ey), ezf = __double2float_rn(ez);
+    if (MOVE) {
+        const float ih = g.inv_h_f;
+        s.u4[sidx(g, sl)] = make_float4(exf * ih, eyf * ih, ezf * ih, __int_as_float(ty));
+    }
+    if (DECIDE) {
         // the exact FP64 test of decide runs only where the FP32 distance is not clearly below it
-        if (DECIDE && !(exf * exf + eyf * eyf + ezf * ezf < g.thr_lo_f)) {
+        bool disp = false;
+        if (!(exf * exf + eyf * eyf + ezf * ezf < g.thr_lo_f)) {
             double dist = __dmul_rn(ex, ex);
             dist = __dadd_rn(dist, __dmul_rn(ey, ey));
             dist = __dadd_rn(dist, __dmul_rn(ez, ez));
             disp = dist > g.thr;
         }
-    }
-    if (DECIDE) {
-        const unsigned m = __ballot_sync(0xffffffffu, disp);
-        if ((threadIdx.x & 31) == 0) in.dmask[t >> 5] = m;
+        in.dflag[t] = disp ? 1 : 0;
     }
 }
 
-// displaced count of each group of kFirstThreads / 32 ballots
+// one warp per group of kFirstThreads flag bytes (8 per lane, read as one 64-bit word): its count
 __global__ void k_disp_count(Inter in, int nblocks) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (b >= nblocks) return;
-    constexpr int kWarps = kFirstThreads / 32;
-    int c = 0;
-    for (int w = 0; w < kWarps; w++) c += __popc(in.dmask[b * kWarps + w]);
-    in.dblock[b] = c;
+    const unsigned long long w = reinterpret_cast<const unsigned long long *>(in.dflag)[b * 32 + (threadIdx.x & 31)];
+    int c = __popcll(w);  // bytes are 0 or 1
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) in.dblock[b] = c;
 }
 
 // one block: block counts -> exclusive offsets (in place), total -> CNT_DISPLACED (clamped to dcap)
@@ -461,22 +461,26 @@ __global__ void __launch_bounds__(1024) k_disp_scan(Inter in, int nblocks) {
     }
 }
 
-// one thread per warp mask: the displaced slots of those 32 threads, in order, at their offsets
-__global__ void k_disp_collect(Geom g, Inter in, int nwarps) {
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (in.cnt[CNT_DISPLACED] == 0 || w >= nwarps) return;
-    unsigned m = in.dmask[w];
-    if (m == 0) return;
-    constexpr int kWarpsPerBlock = kFirstThreads / 32;
-    const int b = w / kWarpsPerBlock;
-    int rank = in.dblock[b];
-    for (int v = b * kWarpsPerBlock; v < w; v++) rank += __popc(in.dmask[v]);
-    while (m) {
-        const int bit = __ffs(m) - 1;
-        m &= m - 1;
+// one warp per group of kFirstThreads flag bytes: its displaced slots, in order, at the group's offset
+__global__ void k_disp_collect(Geom g, Inter in, int nblocks) {
+    if (in.cnt[CNT_DISPLACED] == 0) return;
+    const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (b >= nblocks) return;
+    const int lane = threadIdx.x & 31;
+    unsigned long long w = reinterpret_cast<const unsigned long long *>(in.dflag)[b * 32 + lane];
+    const int c = __popcll(w);
+    int incl = c;  // inclusive scan over the lanes
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (c == 0) return;
+    int rank = in.dblock[b] + incl - c;
+    for (int byte = 0; w; byte++, w >>= 8) {
+        if ((w & 0xff) == 0) continue;
         if (rank < in.dcap) {
             int i, j, k;
-            in.displaced[rank] = local_slot(g, (w << 5) + bit, i, j, k);
+            in.displaced[rank] = local_slot(g, b * kFirstThreads + lane * 8 + byte, i, j, k);
         }
         rank++;
     }
@@ -493,10 +497,10 @@ void launch_decide_scan(const LaunchCtx &lc, const Geom &g, Slots s, Inter in) {
 }
 void launch_displaced_collect(const LaunchCtx &lc, const Geom &g, Inter in) {
     const int nblocks = (g.n_local + kFirstThreads - 1) / kFirstThreads;
-    const int nwarps = nblocks * (kFirstThreads / 32);
-    k_disp_count<<<(nblocks + 255) / 256, 256, 0, lc.stream>>>(in, nblocks);
+    const int grid = (nblocks + 7) / 8;  // 8 warps (groups) per 256-thread block
+    k_disp_count<<<grid, 256, 0, lc.stream>>>(in, nblocks);
     k_disp_scan<<<1, 1024, 0, lc.stream>>>(in, nblocks);
-    k_disp_collect<<<(nwarps + 255) / 256, 256, 0, lc.stream>>>(g, in, nwarps);
+    k_disp_collect<<<grid, 256, 0, lc.stream>>>(g, in, nblocks);
 }
 
 __global__ void k_inter_firststep(Inter in, const StepParams *__restrict__ p) {
