@@ -198,12 +198,13 @@ mg_status mg_ws_map(mg_context *ctx, const double *xyz, int64_t n, int64_t *coor
 
 /* Autotuner: times the density and force passes of the current precision on the resident state for
  * every gather thread order (0: all even sites then all odd; 1: even/odd warps interleaved per 32
- * sites) and block size (128, 256, 512), reps launches each, and keeps the fastest. Results are cached
- * per (box, precision) for the life of the process. out (may be NULL) receives {rho order, rho block,
- * force order, force block}. Needs mg_prepare first. */
-mg_status mg_autotune(mg_context *ctx, int32_t reps, int32_t out[4]);
-/* Sets the four tuning values directly (same layout as mg_autotune's out). */
-mg_status mg_set_tuning(mg_context *ctx, const int32_t tune[4]);
+ * sites), block size (128, 256, 512) and number of sites per thread (1, 2, 4; a thread's sites are
+ * one grid stride apart), reps launches each, and keeps the fastest. Results are cached per
+ * (box, precision) for the life of the process. out (may be NULL) receives {rho order, rho block,
+ * rho sites per thread, force order, force block, force sites per thread}. Needs mg_prepare first. */
+mg_status mg_autotune(mg_context *ctx, int32_t reps, int32_t out[6]);
+/* Sets the six tuning values directly (same layout as mg_autotune's out). */
+mg_status mg_set_tuning(mg_context *ctx, const int32_t tune[6]);
 
 /* Measured kernel times of the last mg_simulate call with timing enabled (ms per step per kernel). */
 mg_status mg_enable_timing(mg_context *ctx, int32_t on);

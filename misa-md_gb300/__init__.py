@@ -397,13 +397,13 @@ class Context:
         return coords, flags, index
 
     def autotune(self, reps=3):
-        out = np.zeros(4, dtype=np.int32)
+        out = np.zeros(6, dtype=np.int32)
         self._check(self.lib.mg_autotune(self.h, int(reps), _ptr(out)))
-        return {"rho_order": int(out[0]), "rho_block": int(out[1]), "force_order": int(out[2]),
-                "force_block": int(out[3])}
+        return {"rho_order": int(out[0]), "rho_block": int(out[1]), "rho_apt": int(out[2]),
+                "force_order": int(out[3]), "force_block": int(out[4]), "force_apt": int(out[5])}
 
-    def set_tuning(self, rho_order, rho_block, force_order, force_block):
-        t = np.asarray([rho_order, rho_block, force_order, force_block], dtype=np.int32)
+    def set_tuning(self, rho_order, rho_block, force_order, force_block, rho_apt=1, force_apt=1):
+        t = np.asarray([rho_order, rho_block, rho_apt, force_order, force_block, force_apt], dtype=np.int32)
         self._check(self.lib.mg_set_tuning(self.h, _ptr(t)))
 
     def enable_timing(self, on=True):

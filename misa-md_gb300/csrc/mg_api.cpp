@@ -20,10 +20,12 @@ namespace {
 
 thread_local std::string g_create_error;
 
-constexpr int kNumTimers = 12;
-const char *kTimerNames[kNumTimers] = {"firststep", "inter_firststep", "inter_manage", "ghost_copy",
-                                       "lat_rho",   "inter_rho",       "lat_df",       "ghost_df",
-                                       "lat_force", "inter_force",     "secondstep",   "far_scatter"};
+constexpr int kNumTimers = 12;  // events per timed step; the kernels between consecutive events are:
+const char *kTimerNames[kNumTimers - 1] = {"firststep",  // step head and firststep
+                                           "inter_firststep",
+                                           "inter_manage",  // displaced collection, far marks and the list manager
+                                           "ghost_copy", "lat_rho", "inter_rho", "lat_df", "ghost_df", "lat_force",
+                                           "inter_force", "secondstep"};
 
 }  // namespace
 
@@ -77,14 +79,17 @@ struct mg_context {
     int64_t timed_steps = 0;
     bool energy_valid = false;
 
-    int tune[2][2][2] = {{{0, 256}, {0, 256}}, {{0, 256}, {0, 256}}};  // [precision][rho, force] = {order, block}
+    // [precision][rho, force] = {thread order, block size, atoms per thread}
+    int tune[2][2][3] = {{{0, 256, 1}, {0, 256, 1}}, {{0, 256, 1}, {0, 256, 1}}};
     LaunchCtx lc() const {
         LaunchCtx l{stream, num_sms};
         l.nt = &nt;
         l.rho_order = tune[precision][0][0];
         l.rho_block = tune[precision][0][1];
+        l.rho_apt = tune[precision][0][2];
         l.force_order = tune[precision][1][0];
         l.force_block = tune[precision][1][1];
+        l.force_apt = tune[precision][1][2];
         return l;
     }
     bool mixed() const { return precision == MG_PREC_MIXED; }
@@ -1111,11 +1116,11 @@ struct TuneKey {
         return cells[0] == o.cells[0] && cells[1] == o.cells[1] && cells[2] == o.cells[2] && precision == o.precision;
     }
 };
-std::vector<std::pair<TuneKey, std::array<int, 4>>> g_tune_cache;
+std::vector<std::pair<TuneKey, std::array<int, 6>>> g_tune_cache;
 std::mutex g_tune_mutex;
 }  // namespace
 
-mg_status mg_autotune(mg_context *ctx, int32_t reps, int32_t out[4]) {
+mg_status mg_autotune(mg_context *ctx, int32_t reps, int32_t out[6]) {
     if (!ctx) return MG_ERR_ARG;
     if (!ctx->prepared) { ctx->err = "mg_prepare must run before mg_autotune"; return MG_ERR_STATE; }
     const int p = ctx->precision;
@@ -1124,8 +1129,9 @@ mg_status mg_autotune(mg_context *ctx, int32_t reps, int32_t out[4]) {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         for (auto &kv : g_tune_cache) {
             if (kv.first == key) {
-                for (int k = 0; k < 2; k++) { ctx->tune[p][k][0] = kv.second[2 * k]; ctx->tune[p][k][1] = kv.second[2 * k + 1]; }
-                if (out) for (int k = 0; k < 4; k++) out[k] = kv.second[k];
+                for (int k = 0; k < 2; k++)
+                    for (int c = 0; c < 3; c++) ctx->tune[p][k][c] = kv.second[3 * k + c];
+                if (out) for (int k = 0; k < 6; k++) out[k] = kv.second[k];
                 ctx->graph_stale = true;
                 ctx->gen++;
                 return MG_OK;
@@ -1136,14 +1142,15 @@ mg_status mg_autotune(mg_context *ctx, int32_t reps, int32_t out[4]) {
     cudaEvent_t e0, e1;
     MG_CK(cudaEventCreate(&e0));
     MG_CK(cudaEventCreate(&e1));
-    const int blocks[3] = {128, 256, 512};
-    std::array<int, 4> best{};
+    const int blocks[3] = {128, 256, 512}, apts[3] = {1, 2, 4};
+    std::array<int, 6> best{};
     for (int kern = 0; kern < 2; kern++) {
         float best_ms = 1e30f;
         for (int order = 0; order < 2; order++) {
-            for (int b : blocks) {
+            for (int b : blocks) for (int apt : apts) {
                 ctx->tune[p][kern][0] = order;
                 ctx->tune[p][kern][1] = b;
+                ctx->tune[p][kern][2] = apt;
                 const LaunchCtx lc = ctx->lc();
                 auto run = [&]() {
                     if (kern == 0) launch_lat_rho(lc, ctx->g, ctx->s, ctx->in, ctx->pt, ctx->mixed(), false);
@@ -1156,11 +1163,10 @@ mg_status mg_autotune(mg_context *ctx, int32_t reps, int32_t out[4]) {
                 MG_CK(cudaEventSynchronize(e1));
                 float ms = 0.f;
                 cudaEventElapsedTime(&ms, e0, e1);
-                if (ms < best_ms) { best_ms = ms; best[2 * kern] = order; best[2 * kern + 1] = b; }
+                if (ms < best_ms) { best_ms = ms; best[3 * kern] = order; best[3 * kern + 1] = b; best[3 * kern + 2] = apt; }
             }
         }
-        ctx->tune[p][kern][0] = best[2 * kern];
-        ctx->tune[p][kern][1] = best[2 * kern + 1];
+        for (int c = 0; c < 3; c++) ctx->tune[p][kern][c] = best[3 * kern + c];
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1170,20 +1176,20 @@ mg_status mg_autotune(mg_context *ctx, int32_t reps, int32_t out[4]) {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         g_tune_cache.push_back({key, best});
     }
-    if (out) for (int k = 0; k < 4; k++) out[k] = best[k];
+    if (out) for (int k = 0; k < 6; k++) out[k] = best[k];
     ctx->graph_stale = true;
     ctx->gen++;  // the captured graph holds the old launch shapes
     return MG_OK;
 }
 
-mg_status mg_set_tuning(mg_context *ctx, const int32_t tune[4]) {
+mg_status mg_set_tuning(mg_context *ctx, const int32_t tune[6]) {
     if (!ctx || !tune) return MG_ERR_ARG;
     for (int k = 0; k < 2; k++) {
-        const int order = tune[2 * k], b = tune[2 * k + 1];
-        if ((order != 0 && order != 1) || (b != 128 && b != 256 && b != 512)) return MG_ERR_ARG;
-        ctx->tune[ctx->precision][k][0] = order;
-        ctx->tune[ctx->precision][k][1] = b;
+        const int order = tune[3 * k], b = tune[3 * k + 1], apt = tune[3 * k + 2];
+        if ((order != 0 && order != 1) || (b != 128 && b != 256 && b != 512) || apt < 1 || apt > 64) return MG_ERR_ARG;
     }
+    for (int k = 0; k < 2; k++)
+        for (int c = 0; c < 3; c++) ctx->tune[ctx->precision][k][c] = tune[3 * k + c];
     ctx->graph_stale = true;
     ctx->gen++;
     return MG_OK;

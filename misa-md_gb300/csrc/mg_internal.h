@@ -24,7 +24,8 @@ constexpr int kSortSmemKeys = 16384;         // bucket keys the list manager sor
 constexpr uint32_t kInBox = 0, kXLow = 1u, kXHigh = 2u, kYLow = 4u, kYHigh = 8u, kZLow = 16u, kZHigh = 32u;
 
 // device counters / flags word indices
-enum { CNT_INTER = 0, CNT_GHOST = 1, CNT_DISPLACED = 2, CNT_ERRORS = 3, CNT_FAR = 4, CNT_WORDS = 8 };
+// CNT_DISP_RAW: displaced slots counted by firststep this step (0 lets the collection kernels skip)
+enum { CNT_INTER = 0, CNT_GHOST = 1, CNT_DISPLACED = 2, CNT_ERRORS = 3, CNT_FAR = 4, CNT_DISP_RAW = 5, CNT_WORDS = 8 };
 
 inline double atom_mass(int type) {  // src/types/atom_types.h:42-53
     switch (type) {
@@ -203,8 +204,8 @@ struct NeighTables {
 struct LaunchCtx {
     cudaStream_t stream;
     int num_sms;
-    int rho_order = 0, rho_block = 256;      // gather thread order and block size of the density pass
-    int force_order = 0, force_block = 256;  // the same for the force pass (chosen by mg_autotune)
+    int rho_order = 0, rho_block = 256, rho_apt = 1;        // gather thread order, block size and atoms per thread
+    int force_order = 0, force_block = 256, force_apt = 1;  // of the density and force passes (mg_autotune)
     const NeighTables *nt = nullptr;         // the context's offset tables
 };
 

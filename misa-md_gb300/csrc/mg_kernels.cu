@@ -339,6 +339,7 @@ __global__ void k_set_counts(Inter in, int n_inter) {
     in.cnt[CNT_INTER] = n_inter;
     in.cnt[CNT_GHOST] = 0;
     in.cnt[CNT_DISPLACED] = 0;
+    in.cnt[CNT_DISP_RAW] = 0;
     *in.n_bucket = 0;
 }
 void launch_set_counts(const LaunchCtx &lc, Inter in, int n_inter) { k_set_counts<<<1, 1, 0, lc.stream>>>(in, n_inter); }
@@ -364,6 +365,17 @@ void launch_site_table(const LaunchCtx &lc, const Geom &g, double *site_half) {
 // (thread t holds local slot t in k, j, i order; 1 = displaced). A count kernel sums the bytes of each
 // group of kFirstThreads slots, a one-block scan turns the sums into offsets, and a collect kernel
 // writes the slots in order. firststep keeps its early exits and needs no warp or block collective.
+// decide's distance test (src/atom.cpp:34-42) with each operation rounded on its own; a displaced
+// atom also counts itself into CNT_DISP_RAW, so the collection kernels can skip steps without any
+__device__ __noinline__ bool exact_displaced(double ex, double ey, double ez, double thr, int *raw_count) {
+    double dist = __dmul_rn(ex, ex);
+    dist = __dadd_rn(dist, __dmul_rn(ey, ey));
+    dist = __dadd_rn(dist, __dmul_rn(ez, ez));
+    const bool d = dist > thr;
+    if (d) atomicAdd(raw_count, 1);
+    return d;
+}
+
 template <bool MOVE, bool DECIDE>
 __global__ void __launch_bounds__(kFirstThreads) k_firststep(Geom g, Slots s, Inter in, const StepParams *__restrict__ p) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -401,19 +413,16 @@ __global__ void __launch_bounds__(kFirstThreads) k_firststep(Geom g, Slots s, In
     }
     if (DECIDE) {
         // the exact FP64 test of decide runs only where the FP32 distance is not clearly below it
-        bool disp = false;
-        if (!(exf * exf + eyf * eyf + ezf * ezf < g.thr_lo_f)) {
-            double dist = __dmul_rn(ex, ex);
-            dist = __dadd_rn(dist, __dmul_rn(ey, ey));
-            dist = __dadd_rn(dist, __dmul_rn(ez, ez));
-            disp = dist > g.thr;
-        }
+        // (a call, so the rare path stays a branch instead of being evaluated for every atom)
+        const bool disp = !(exf * exf + eyf * eyf + ezf * ezf < g.thr_lo_f) &&
+                          exact_displaced(ex, ey, ez, g.thr, &in.cnt[CNT_DISP_RAW]);
         in.dflag[t] = disp ? 1 : 0;
     }
 }
 
 // one warp per group of kFirstThreads flag bytes (8 per lane, read as one 64-bit word): its count
 __global__ void k_disp_count(Inter in, int nblocks) {
+    if (in.cnt[CNT_DISP_RAW] == 0) return;  // nothing displaced this step (the usual case)
     const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (b >= nblocks) return;
     const unsigned long long w = reinterpret_cast<const unsigned long long *>(in.dflag)[b * 32 + (threadIdx.x & 31)];
@@ -426,6 +435,10 @@ __global__ void k_disp_count(Inter in, int nblocks) {
 __global__ void __launch_bounds__(1024) k_disp_scan(Inter in, int nblocks) {
     __shared__ int warp_tot[32];
     __shared__ int running;
+    if (in.cnt[CNT_DISP_RAW] == 0) {  // nothing displaced this step (the usual case)
+        if (threadIdx.x == 0) in.cnt[CNT_DISPLACED] = 0;
+        return;
+    }
     if (threadIdx.x == 0) running = 0;
     __syncthreads();
     for (int c0 = 0; c0 < nblocks; c0 += blockDim.x) {
@@ -458,6 +471,7 @@ __global__ void __launch_bounds__(1024) k_disp_scan(Inter in, int nblocks) {
         int total = running;
         if (total > in.dcap) { set_error(in, MG_DEVERR_DISPLACED_OVERFLOW); total = in.dcap; }
         in.cnt[CNT_DISPLACED] = total;
+        in.cnt[CNT_DISP_RAW] = 0;
     }
 }
 
@@ -635,8 +649,7 @@ __device__ __forceinline__ double rho_sum_fp64(const NeighTables &nt, const Geom
     return acc;
 }
 
-__global__ void __launch_bounds__(512) k_lat_rho_fp64(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool hook, int order) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_lat_rho_fp64_site(int t, const NeighTables &nt, const Geom &g, const Slots &s, const Inter &in, const PotTables &pt, bool hook, int order) {
     int par;
     const int sl = gather_slot(g, t, order, par);
     if (sl < 0) return;
@@ -659,6 +672,15 @@ __global__ void __launch_bounds__(512) k_lat_rho_fp64(const __grid_constant__ Ne
         locate_d(acc, pt.inv_drho, pt.nrho, m, p);
         s.df[sl] = der_d(pt.F_d + ti * pt.nrho, m, p);
     }
+}
+template <bool LOOP>  // LOOP: several sites per thread, one grid stride apart
+__global__ void __launch_bounds__(512) k_lat_rho_fp64(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool hook, int order, int nthreads) {
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!LOOP) {
+        if (t0 < nthreads) k_lat_rho_fp64_site(t0, nt, g, s, in, pt, hook, order);
+        return;
+    }
+    for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x) k_lat_rho_fp64_site(t, nt, g, s, in, pt, hook, order);
 }
 
 template <int PAR>
@@ -687,8 +709,7 @@ __device__ __forceinline__ void rho_sum_mixed(const NeighTables &nt, const Geom 
     }
 }
 
-__global__ void __launch_bounds__(512) k_lat_rho_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool hook, int order) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_lat_rho_mixed_site(int t, const NeighTables &nt, const Geom &g, const Slots &s, const Inter &in, const PotTables &pt, bool hook, int order) {
     int par;
     const int sl = gather_slot(g, t, order, par);
     if (sl < 0) return;
@@ -713,11 +734,28 @@ __global__ void __launch_bounds__(512) k_lat_rho_mixed(const __grid_constant__ N
         s.df32[si] = der_f(pt.F_dff + ti * pt.nrho, m, p);
     }
 }
+template <bool LOOP>  // LOOP: several sites per thread, one grid stride apart
+__global__ void __launch_bounds__(512) k_lat_rho_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool hook, int order, int nthreads) {
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!LOOP) {
+        if (t0 < nthreads) k_lat_rho_mixed_site(t0, nt, g, s, in, pt, hook, order);
+        return;
+    }
+    for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x) k_lat_rho_mixed_site(t, nt, g, s, in, pt, hook, order);
+}
 
 void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook) {
-    const int order = lc.rho_order, b = lc.rho_block, n = (gather_threads(g, order) + b - 1) / b;
-    if (mixed) k_lat_rho_mixed<<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order);
-    else k_lat_rho_fp64<<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order);
+    // atoms per thread: each thread takes rho_apt sites, one grid stride apart (the stride is a
+    // multiple of 64, so warps keep their parity and thread order)
+    const int order = lc.rho_order, b = lc.rho_block, nthr = gather_threads(g, order);
+    const int n = (nthr + b * lc.rho_apt - 1) / (b * lc.rho_apt);
+    if (lc.rho_apt > 1) {
+        if (mixed) k_lat_rho_mixed<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, nthr);
+        else k_lat_rho_fp64<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, nthr);
+    } else {
+        if (mixed) k_lat_rho_mixed<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, nthr);
+        else k_lat_rho_fp64<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, nthr);
+    }
 }
 
 // dF/drho when inter atoms added density after the lattice pass (or for the df hook)
@@ -789,9 +827,8 @@ __device__ __forceinline__ void force_sum_fp64(const NeighTables &nt, const Geom
     }
 }
 
-__global__ void __launch_bounds__(512) k_lat_force_fp64(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, StepParams *sp,
-                                                        bool kick, bool hook, int order) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_lat_force_fp64_site(int t, const NeighTables &nt, const Geom &g, const Slots &s, const Inter &in,
+                                                const PotTables &pt, StepParams *sp, bool kick, bool hook, int order) {
     int par;
     const int sl = gather_slot(g, t, order, par);
     if (sl < 0) return;
@@ -819,6 +856,16 @@ __global__ void __launch_bounds__(512) k_lat_force_fp64(const __grid_constant__ 
         s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz;
         note_vmax2(sp, speed2(vx, vy, vz));
     }
+}
+template <bool LOOP>  // LOOP: several sites per thread, one grid stride apart
+__global__ void __launch_bounds__(512) k_lat_force_fp64(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt,
+                                                         StepParams *sp, bool kick, bool hook, int order, int nthreads) {
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!LOOP) {
+        if (t0 < nthreads) k_lat_force_fp64_site(t0, nt, g, s, in, pt, sp, kick, hook, order);
+        return;
+    }
+    for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x) k_lat_force_fp64_site(t, nt, g, s, in, pt, sp, kick, hook, order);
 }
 
 template <int PAR>
@@ -865,9 +912,8 @@ __device__ __forceinline__ void force_sum_mixed(const NeighTables &nt, const Geo
     }
 }
 
-__global__ void __launch_bounds__(512, 3) k_lat_force_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, StepParams *sp,
-                                                         bool kick, bool hook, int order) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables &nt, const Geom &g, const Slots &s, const Inter &in,
+                                                const PotTables &pt, StepParams *sp, bool kick, bool hook, int order) {
     int par;
     const int sl = gather_slot(g, t, order, par);
     if (sl < 0) return;
@@ -904,12 +950,28 @@ __global__ void __launch_bounds__(512, 3) k_lat_force_mixed(const __grid_constan
         note_vmax2(sp, speed2(vx, vy, vz));
     }
 }
+template <bool LOOP>  // LOOP: several sites per thread, one grid stride apart
+__global__ void __launch_bounds__(512, 3) k_lat_force_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt,
+                                                         StepParams *sp, bool kick, bool hook, int order, int nthreads) {
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!LOOP) {
+        if (t0 < nthreads) k_lat_force_mixed_site(t0, nt, g, s, in, pt, sp, kick, hook, order);
+        return;
+    }
+    for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x) k_lat_force_mixed_site(t, nt, g, s, in, pt, sp, kick, hook, order);
+}
 
 void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *p, bool kick,
                       bool mixed, bool hook) {
-    const int order = lc.force_order, b = lc.force_block, n = (gather_threads(g, order) + b - 1) / b;
-    if (mixed) k_lat_force_mixed<<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order);
-    else k_lat_force_fp64<<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order);
+    const int order = lc.force_order, b = lc.force_block, nthr = gather_threads(g, order);
+    const int n = (nthr + b * lc.force_apt - 1) / (b * lc.force_apt);
+    if (lc.force_apt > 1) {
+        if (mixed) k_lat_force_mixed<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, nthr);
+        else k_lat_force_fp64<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, nthr);
+    } else {
+        if (mixed) k_lat_force_mixed<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, nthr);
+        else k_lat_force_fp64<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, nthr);
+    }
 }
 
 // second half-kick for lattice slots (only when inter atoms prevented fusion, or always) and for

@@ -395,14 +395,14 @@ def test_autotune_keeps_results_bit_identical(pkg, wl, potentials, gpu_lib, prec
     cells = (14, 12, 13)
     atoms = wl.build_state(cells, A0, RCF, temperature=600.0, seed=81, cu_frac=0.02, ni_frac=0.01)
     runs = []
-    for tune in (None, (1, 128, 1, 512), "auto"):
+    for tune in (None, (1, 128, 1, 512), (0, 256, 1, 128, 2, 4), "auto"):
         ctx = pkg.Context(cells, A0, RCF, precision=prec)
         ctx.pot_init_setfl(potentials["fecuni"])
         ctx.upload(atoms)
         ctx.prepare()
         if tune == "auto":
             t = ctx.autotune(reps=2)
-            assert t["rho_order"] in (0, 1) and t["force_block"] in (128, 256, 512)
+            assert t["rho_order"] in (0, 1) and t["force_block"] in (128, 256, 512) and t["force_apt"] in (1, 2, 4)
         elif tune is not None:
             ctx.set_tuning(*tune)
         ctx.simulate(5)
