@@ -277,6 +277,48 @@ mg_status mg_world_build(const int64_t phase_space[3], double lattice_const, dou
                          double t_set, uint32_t seed, const int32_t alloy_ratio[3], int32_t rng,
                          mg_atom_element *atoms, int64_t n_slots);
 
+/* ---- Atom dump (AtomDump::dump / writeDumpHeader, frontend/io/atom_dump.cpp:38-82; OutputCopy,
+ * frontend/io/output_copy.cpp:19-59; records as BufferedFileWriter::write,
+ * frontend/io/buffered_io.cpp:17-35) ----
+ * Binary frames in the copy-mode file layout that tools/dump2text/out_convert.cpp:66-98 reads for
+ * one rank: a 128-byte file header (kiwi::LocalStorage's own; no reader uses it, written as zeros),
+ * a 128-byte rank header whose first 8 bytes hold the number of records in the file, then the
+ * 72-byte records. A frame holds the context's inter atoms in list order, then the lattice atoms of
+ * the box in k, j, i order without vacant slots, each with the time step given; inter_type is 0 for
+ * every record, as the reference writes it.
+ *   by_frame == 0: one file at path; frames are appended and mg_dump_close writes the header
+ *                  (OutputCopy without by_frame).
+ *   by_frame != 0: path holds "{}", replaced by the time step of each frame; one file per frame,
+ *                  each with its header (output_copy.cpp:28-33).
+ * A frame is packed on the device (ordered compaction) into one of two staging buffers; a writer
+ * thread copies it through two pinned chunks of chunk_bytes (0: 64 MiB) and writes chunk k while
+ * chunk k + 1 is in flight. mg_dump_frame returns once the frame is enqueued on the context's stream;
+ * it waits only while both staging buffers still hold unwritten frames. A dump belongs to one
+ * context: close it (or detach it from the stage machine) before destroying the context. ---- */
+typedef struct mg_dump_record {
+    uint64_t id;
+    uint64_t step;
+    int32_t type;
+    int16_t inter_type;
+    int16_t pad_;
+    double x[3];
+    double v[3];
+} mg_dump_record;
+typedef struct mg_dump mg_dump;
+mg_status mg_dump_open(mg_context *ctx, const char *path, int32_t by_frame, int64_t chunk_bytes, mg_dump **out);
+mg_status mg_dump_frame(mg_dump *d, uint64_t time_step);
+/* Waits for every frame, writes the header, closes the file and frees d (also after an error).
+ * *records (may be NULL): records written (single file: the header's count; by_frame: all frames).
+ * An I/O or CUDA failure of any frame is returned here and by the next mg_dump_frame. */
+mg_status mg_dump_close(mg_dump *d, uint64_t *records);
+const char *mg_dump_last_error(const mg_dump *d);
+/* Dumps of the stage machine (MDSimulation::beforeStep / postStep, frontend/md_simulation.cpp:64-70,
+ * 86-90): mg_run_stages appends a frame to `frames` (NULL: none) after every step whose 1-based
+ * number is a multiple of interval, with that number as its time step, and before each collision
+ * writes the state to origin_path (NULL or "": none) as a one-frame file whose time step is the
+ * 0-based number of the step about to run (OutputCopy::beforeCollision). */
+mg_status mg_set_stage_output(mg_context *ctx, mg_dump *frames, uint64_t interval, const char *origin_path);
+
 /* Page-lock a host range (the caller's slot array) so mg_step_host / mg_upload / mg_download copy it
  * by DMA; undo with mg_host_unregister before freeing it. */
 mg_status mg_host_register(void *ptr, uint64_t bytes);

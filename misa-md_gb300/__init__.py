@@ -31,6 +31,7 @@ def _load_sibling(name):
 
 workloads = _load_sibling("workloads")
 build = _load_sibling("build")
+dumpfile = _load_sibling("dumpfile")
 ATOM_DTYPE = workloads.ATOM_DTYPE
 
 PREC = {"fp64": 0, "mixed": 1}
@@ -117,6 +118,11 @@ _PROTOS = {
     "mg_mvv_noalloc": (_I32, [_P, _P, _P, _P, _I64, _P, _P]),
     "mg_autotune": (_I32, [_P, _I32, _P]),
     "mg_set_tuning": (_I32, [_P, _P]),
+    "mg_dump_open": (_I32, [_P, ctypes.c_char_p, _I32, _I64, _P]),
+    "mg_dump_frame": (_I32, [_P, _U64]),
+    "mg_dump_close": (_I32, [_P, _P]),
+    "mg_dump_last_error": (ctypes.c_char_p, [_P]),
+    "mg_set_stage_output": (_I32, [_P, _P, _U64, ctypes.c_char_p]),
 }
 
 
@@ -264,10 +270,20 @@ class Context:
         """dt = clamp(dx_max / max|v|, dt_min, dt_max) before every step (Angstrom, ps)."""
         self._check(self.lib.mg_set_variable_timestep(self.h, float(dx_max), float(dt_min), float(dt_max)))
 
+    def dump_open(self, path, by_frame=False, chunk_bytes=0):
+        """An atom dump of this context in the reference's copy-mode layout (mg_dump_open)."""
+        return Dump(self, path, by_frame, chunk_bytes)
+
+    def set_stage_output(self, dump=None, interval=0, origin_path=None):
+        """Dumps taken by run_stages: a frame into `dump` after every interval-th step, and the state
+        before each collision into origin_path (mg_set_stage_output)."""
+        self._check(self.lib.mg_set_stage_output(self.h, dump.h if dump is not None else None, int(interval),
+                                                 os.fsencode(origin_path) if origin_path else None))
+
     def run_stages(self, stages, steps, default_dt, n_atoms, thermo_interval=0):
         """The reference's stage driver (MDSimulation::beforeStep / postStep) on the device. stages: dicts
         with steps, step_length, and optionally collision_step + lat + direction + energy and
-        rescale_t + rescale_every. Returns the thermo samples as dicts."""
+        rescale_t + rescale_every. Returns the thermo samples as dicts. Dumps as set_stage_output set."""
         arr = (StageIn * max(1, len(stages)))()
         for k, st in enumerate(stages):
             a = arr[k]
@@ -423,6 +439,48 @@ class Context:
 
     def stream(self):
         return self.lib.mg_stream(self.h)
+
+
+class Dump:
+    """Binary atom dump fed from the device (mg_dump_*): frames are packed on the GPU and written by a
+    background thread. by_frame: path holds "{}" for the time step, one file per frame."""
+
+    def __init__(self, ctx, path, by_frame=False, chunk_bytes=0):
+        self.lib = ctx.lib
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        st = self.lib.mg_dump_open(ctx.h, os.fsencode(path), 1 if by_frame else 0, int(chunk_bytes), ctypes.byref(h))
+        if st != 0:
+            raise MgError(st, f"cannot open dump {path}")
+        self.h = h
+
+    def frame(self, time_step):
+        st = self.lib.mg_dump_frame(self.h, int(time_step))
+        if st != 0:
+            raise MgError(st, (self.lib.mg_dump_last_error(self.h) or b"").decode())
+
+    def close(self):
+        """Waits for every frame and writes the header; returns the records written."""
+        if not getattr(self, "h", None):
+            return None
+        n = ctypes.c_uint64(0)
+        h, self.h = self.h, None
+        st = self.lib.mg_dump_close(h, ctypes.byref(n))
+        if st != 0:
+            raise MgError(st, (self.lib.mg_last_error(self.ctx.h) or b"").decode())
+        return n.value
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Batch:

@@ -14,7 +14,8 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libmisa_gb300.so")
-SOURCES = ["csrc/mg_kernels.cu", "csrc/mg_api.cpp", "csrc/mg_potential.cpp", "csrc/mg_noalloc.cu", "csrc/mg_world.cpp"]
+SOURCES = ["csrc/mg_kernels.cu", "csrc/mg_api.cpp", "csrc/mg_potential.cpp", "csrc/mg_noalloc.cu", "csrc/mg_world.cpp",
+           "csrc/mg_dump.cpp"]
 HEADERS = ["csrc/mg_internal.h", "../include/misa_gb300.h"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC,-ffp-contract=off"]
@@ -59,7 +60,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             if verbose and out.strip():
                 print(out)
     tmp = LIB_PATH + f".tmp{os.getpid()}"
-    run([cc, *NVCC_FLAGS, "-shared", "-o", tmp, *objs, "-lcudart"])
+    run([cc, *NVCC_FLAGS, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread"])
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 

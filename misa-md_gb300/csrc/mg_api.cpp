@@ -78,6 +78,10 @@ struct mg_context {
     std::vector<double> timer_ms;      // accumulated per kernel
     int64_t timed_steps = 0;
     bool energy_valid = false;
+    // stage-machine dumps (mg_set_stage_output)
+    mg_dump *stage_dump = nullptr;
+    uint64_t stage_dump_interval = 0;
+    std::string origin_path;
 
     // [precision][rho, force] = {thread order, block size, atoms per thread}
     int tune[2][2][3] = {{{0, 256, 1}, {0, 256, 1}}, {{0, 256, 1}, {0, 256, 1}}};
@@ -938,6 +942,47 @@ mg_status mg_rescale(mg_context *ctx, double t_set, uint64_t n_atoms) {
 // MDSimulation::beforeStep / postStep (frontend/md_simulation.cpp:40-111) around the loop body, all on
 // the context's stream: stage changes set dt on the device, rescales and PKAs are kernels, steps are
 // graph replays, thermo samples go to a device buffer read once at the end.
+// OutputCopy::beforeCollision (frontend/io/output_copy.cpp:41-49): the state before the PKA as a
+// one-frame file
+static mg_status dump_origin(mg_context *ctx, uint64_t time_step) {
+    mg_dump *d = nullptr;
+    mg_status st = mg_dump_open(ctx, ctx->origin_path.c_str(), 0, 0, &d);
+    if (st != MG_OK) return st;
+    st = mg_dump_frame(d, time_step);
+    std::string why = st != MG_OK ? mg_dump_last_error(d) : "";
+    const mg_status st2 = mg_dump_close(d, nullptr);
+    if (st == MG_OK) st = st2;
+    if (st != MG_OK) ctx->err = "origin dump: " + (why.empty() ? ctx->err : why);
+    return st;
+}
+
+mg_status mg_set_stage_output(mg_context *ctx, mg_dump *frames, uint64_t interval, const char *origin_path) {
+    if (!ctx) return MG_ERR_ARG;
+    ctx->stage_dump = frames;
+    ctx->stage_dump_interval = frames ? interval : 0;
+    ctx->origin_path = origin_path ? origin_path : "";
+    return MG_OK;
+}
+
+extern "C++" {
+namespace mg {
+DumpSource dump_source(const mg_context *ctx) {
+    return DumpSource{ctx->stream, static_cast<int64_t>(ctx->g.n_local) + ctx->in.cap, dump_scratch_ints(ctx->g)};
+}
+mg_status dump_pack(mg_context *ctx, mg_dump_record *out, unsigned long long *count, int *scratch, uint64_t step) {
+    launch_dump_pack(ctx->lc(), ctx->g, ctx->s, ctx->in, out, count, scratch, step);
+    return check_launch(ctx);
+}
+void dump_note_error(mg_context *ctx, const std::string &why) { ctx->err = why; }
+void dump_detach(mg_context *ctx, const mg_dump *d) {
+    if (ctx->stage_dump == d) {
+        ctx->stage_dump = nullptr;
+        ctx->stage_dump_interval = 0;
+    }
+}
+}  // namespace mg
+}  // extern "C++"
+
 mg_status mg_run_stages(mg_context *ctx, const mg_stage *stages, int32_t n_stages, int64_t steps, double default_dt,
                         int64_t n_atoms, int32_t thermo_interval, mg_thermo_sample *samples, int64_t cap,
                         int64_t *n_samples) {
@@ -979,6 +1024,7 @@ mg_status mg_run_stages(mg_context *ctx, const mg_stage *stages, int32_t n_stage
             set_dt(ctx, cur->step_length == 0.0 ? default_dt : cur->step_length);
         }
         if (cur->collision_set && cur_stage_steps + 1 == cur->collision_step) {
+            if (!ctx->origin_path.empty() && (st = dump_origin(ctx, static_cast<uint64_t>(step))) != MG_OK) return st;
             if ((st = enqueue_collision(ctx, cur->collision_lat, cur->direction, cur->pka_energy)) != MG_OK) return st;
         }
         if (cur->rescales_set && cur_stage_steps % cur->rescale_every == 0) {
@@ -992,6 +1038,12 @@ mg_status mg_run_stages(mg_context *ctx, const mg_stage *stages, int32_t n_stage
         }
         MG_CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
         cur_stage_steps++;
+        if (ctx->stage_dump && ctx->stage_dump_interval && (step + 1) % ctx->stage_dump_interval == 0) {
+            if ((st = mg_dump_frame(ctx->stage_dump, static_cast<uint64_t>(step + 1))) != MG_OK) {
+                ctx->err = std::string("dump: ") + mg_dump_last_error(ctx->stage_dump);
+                return st;
+            }
+        }
         if (thermo_interval && (step + 1) % thermo_interval == 0) {
             double *rec = ctx->d_samples + kWords * taken;
             launch_thermo(lc, ctx->g, ctx->s, ctx->in, false, ctx->d_partials, ctx->n_partials, rec);

@@ -260,5 +260,22 @@ void launch_thermo(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool w
                    int n_partials, double *out);
 void launch_ws_map(const LaunchCtx &lc, const Geom &g, const double *xyz, int64_t n, int64_t *coords, uint32_t *flags,
                    int64_t *index);
+// atom dump: the records of one frame (inter atoms in list order, then the box's lattice atoms in
+// k, j, i order without vacancies) into out; *count = records. scratch: dump_scratch_ints(g) ints.
+constexpr int kDumpThreads = 256;
+inline int dump_scratch_ints(const Geom &g) { return (g.n_local + kDumpThreads - 1) / kDumpThreads; }
+void launch_dump_pack(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, mg_dump_record *out,
+                      unsigned long long *count, int *scratch, uint64_t step);
+
+// mg_api.cpp services for the dump writer (mg_dump.cpp)
+struct DumpSource {
+    cudaStream_t stream;
+    int64_t max_records;   // local slots + inter-atom capacity
+    int scratch_ints;
+};
+DumpSource dump_source(const mg_context *ctx);
+mg_status dump_pack(mg_context *ctx, mg_dump_record *out, unsigned long long *count, int *scratch, uint64_t step);
+void dump_detach(mg_context *ctx, const mg_dump *d);  // mg_dump_close: the stage machine forgets d
+void dump_note_error(mg_context *ctx, const std::string &why);  // mg_last_error(ctx) reports it
 
 }  // namespace mg

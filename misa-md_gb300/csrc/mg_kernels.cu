@@ -431,19 +431,15 @@ __global__ void k_disp_count(Inter in, int nblocks) {
     if ((threadIdx.x & 31) == 0) in.dblock[b] = c;
 }
 
-// one block: block counts -> exclusive offsets (in place), total -> CNT_DISPLACED (clamped to dcap)
-__global__ void __launch_bounds__(1024) k_disp_scan(Inter in, int nblocks) {
+// one block: counts a[0..n) -> base + exclusive offsets (in place); returns base + the total (every thread)
+__device__ int block_scan_counts(int *a, int n, int base) {
     __shared__ int warp_tot[32];
     __shared__ int running;
-    if (in.cnt[CNT_DISP_RAW] == 0) {  // nothing displaced this step (the usual case)
-        if (threadIdx.x == 0) in.cnt[CNT_DISPLACED] = 0;
-        return;
-    }
-    if (threadIdx.x == 0) running = 0;
+    if (threadIdx.x == 0) running = base;
     __syncthreads();
-    for (int c0 = 0; c0 < nblocks; c0 += blockDim.x) {
+    for (int c0 = 0; c0 < n; c0 += blockDim.x) {
         const int b = c0 + threadIdx.x;
-        const int v = b < nblocks ? in.dblock[b] : 0;
+        const int v = b < n ? a[b] : 0;
         int x = v;  // inclusive warp scan
         for (int o = 1; o < 32; o <<= 1) {
             const int y = __shfl_up_sync(0xffffffffu, x, o);
@@ -461,14 +457,23 @@ __global__ void __launch_bounds__(1024) k_disp_scan(Inter in, int nblocks) {
         }
         __syncthreads();
         const int warp_base = (threadIdx.x >> 5) ? warp_tot[(threadIdx.x >> 5) - 1] : 0;
-        const int base = running;
-        if (b < nblocks) in.dblock[b] = base + warp_base + x - v;
+        const int cur = running;
+        if (b < n) a[b] = cur + warp_base + x - v;
         __syncthreads();
-        if (threadIdx.x == 0) running = base + warp_tot[(blockDim.x >> 5) - 1];
+        if (threadIdx.x == 0) running = cur + warp_tot[(blockDim.x >> 5) - 1];
         __syncthreads();
     }
+    return running;
+}
+
+// one block: block counts -> exclusive offsets (in place), total -> CNT_DISPLACED (clamped to dcap)
+__global__ void __launch_bounds__(1024) k_disp_scan(Inter in, int nblocks) {
+    if (in.cnt[CNT_DISP_RAW] == 0) {  // nothing displaced this step (the usual case)
+        if (threadIdx.x == 0) in.cnt[CNT_DISPLACED] = 0;
+        return;
+    }
+    int total = block_scan_counts(in.dblock, nblocks, 0);
     if (threadIdx.x == 0) {
-        int total = running;
         if (total > in.dcap) { set_error(in, MG_DEVERR_DISPLACED_OVERFLOW); total = in.dcap; }
         in.cnt[CNT_DISPLACED] = total;
         in.cnt[CNT_DISP_RAW] = 0;
@@ -1821,6 +1826,70 @@ void launch_ws_map(const LaunchCtx &lc, const Geom &g, const double *xyz, int64_
                    int64_t *index) {
     const int b = 256;
     k_ws_map<<<(unsigned) ((n + b - 1) / b), b, 0, lc.stream>>>(g, xyz, n, coords, flags, index);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Atom dump frames (AtomDump::dump, frontend/io/atom_dump.cpp:59-81, with the record of
+// BufferedFileWriter::write, frontend/io/buffered_io.cpp:17-35): inter atoms in list order first, then
+// the box's lattice atoms in k, j, i order without INVALID slots. An ordered compaction over groups of
+// kDumpThreads local slots: count, one-block scan (offsets start after the inter atoms), write.
+// ------------------------------------------------------------------------------------------------
+static_assert(sizeof(mg_dump_record) == 72, "dump record layout (tools/dump2text/out_convert.cpp:18-25)");
+
+__device__ __forceinline__ void put_dump_record(mg_dump_record *r, uint64_t id, uint64_t step, int type, double x,
+                                                double y, double z, double vx, double vy, double vz) {
+    mg_dump_record q;
+    q.id = id;
+    q.step = step;
+    q.type = type;
+    q.inter_type = 0;  // BufferedFileWriter::write sets 0 for every record
+    q.pad_ = 0;
+    q.x[0] = x; q.x[1] = y; q.x[2] = z;
+    q.v[0] = vx; q.v[1] = vy; q.v[2] = vz;
+    *r = q;
+}
+__global__ void __launch_bounds__(kDumpThreads) k_dump_count(Geom g, Slots s, int *group_count) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int live = 0;
+    if (t < g.n_local) {
+        int i, j, k;
+        live = s.type[local_slot(g, t, i, j, k)] >= 0;
+    }
+    const int c = __syncthreads_count(live);
+    if (threadIdx.x == 0) group_count[blockIdx.x] = c;
+}
+__global__ void __launch_bounds__(1024) k_dump_scan(Inter in, int *group_count, int ngroups, unsigned long long *count) {
+    const int n_inter = min(in.cnt[CNT_INTER], in.cap);
+    const int total = block_scan_counts(group_count, ngroups, n_inter);
+    if (threadIdx.x == 0) *count = (unsigned long long) total;
+}
+__global__ void __launch_bounds__(kDumpThreads) k_dump_write(Geom g, Slots s, const int *group_offset, mg_dump_record *out,
+                                                             uint64_t step) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int sl = -1;
+    if (t < g.n_local) {
+        int i, j, k;
+        sl = local_slot(g, t, i, j, k);
+        if (s.type[sl] < 0) sl = -1;
+    }
+    int pos;
+    block_exclusive_scan(sl >= 0 ? 1 : 0, pos);
+    if (sl < 0) return;
+    put_dump_record(out + group_offset[blockIdx.x] + pos, s.id[sl], step, s.type[sl], s.x[sl], s.y[sl], s.z[sl], s.vx[sl],
+                    s.vy[sl], s.vz[sl]);
+}
+__global__ void k_dump_inter(Inter in, mg_dump_record *out, uint64_t step) {
+    const int n = min(in.cnt[CNT_INTER], in.cap);
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x)
+        put_dump_record(out + a, in.id[a], step, in.type[a], in.x[a], in.y[a], in.z[a], in.vx[a], in.vy[a], in.vz[a]);
+}
+void launch_dump_pack(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, mg_dump_record *out,
+                      unsigned long long *count, int *scratch, uint64_t step) {
+    const int ngroups = dump_scratch_ints(g);
+    k_dump_count<<<ngroups, kDumpThreads, 0, lc.stream>>>(g, s, scratch);
+    k_dump_scan<<<1, 1024, 0, lc.stream>>>(in, scratch, ngroups, count);
+    k_dump_write<<<ngroups, kDumpThreads, 0, lc.stream>>>(g, s, scratch, out, step);
+    k_dump_inter<<<lc.num_sms, 256, 0, lc.stream>>>(in, out, step);
 }
 
 }  // namespace mg

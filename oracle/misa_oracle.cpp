@@ -1281,6 +1281,31 @@ int32_t orc_pot_spline(const orc_sim *s, int32_t kind, int32_t e1, int32_t e2, d
     return sp.n;
 }
 
+int64_t orc_dump_records(const orc_sim *s, uint64_t time_step, orc_dump_record *out, int64_t cap) {
+    int64_t n = 0;
+    auto put = [&](const orc_atom &a) {
+        if (n < cap) {
+            orc_dump_record &r = out[n];
+            std::memset(&r, 0, sizeof(r));
+            r.id = a.id;
+            r.step = time_step;
+            r.type = a.type;
+            r.inter_type = 0;  // "normal", as the reference writes it for every atom
+            for (int d = 0; d < 3; d++) { r.x[d] = a.x[d]; r.v[d] = a.v[d]; }
+        }
+        n++;
+    };
+    for (const orc_atom &a : s->inter_list) put(a);
+    const Domain &d = s->dom;  // the sub-box in ghost coordinates, z outermost
+    for (int64_t k = d.dbx_ghost[2]; k < d.dbx_sub_size[2] + d.dbx_ghost[2]; k++)
+        for (int64_t j = d.dbx_ghost[1]; j < d.dbx_sub_size[1] + d.dbx_ghost[1]; j++)
+            for (int64_t i = d.dbx_ghost[0]; i < d.dbx_sub_size[0] + d.dbx_ghost[0]; i++) {
+                const orc_atom &a = s->atoms[s->idx(i, j, k)];
+                if (a.type != kInvalid) put(a);
+            }
+    return n;
+}
+
 double orc_time_simulate(orc_sim *s, int64_t nsteps) {
     const auto t0 = std::chrono::steady_clock::now();
     for (int64_t i = 0; i < nsteps; i++) s->step();

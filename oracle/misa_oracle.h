@@ -134,6 +134,21 @@ double orc_pot_pair(const orc_sim *s, int32_t key_i, int32_t key_j, double r2);
  * second element. Writes 7*n doubles (c0,c1,c2,c3,d0,d1,d2 per knot). Returns n. */
 int32_t orc_pot_spline(const orc_sim *s, int32_t kind, int32_t e1, int32_t e2, double *out, int32_t cap);
 
+/* Atom dump records (AtomDump::dump, frontend/io/atom_dump.cpp:59-81; BufferedFileWriter::write,
+ * frontend/io/buffered_io.cpp:17-35): the inter atoms in list order, then the sub-box lattice atoms in
+ * k, j, i order without INVALID slots; each record {id, step, type, inter_type = 0, x, v}, 72 bytes
+ * (the layout tools/dump2text/out_convert.cpp:18-25 reads). Writes min(n, cap); returns n. */
+typedef struct orc_dump_record {
+    uint64_t id;
+    uint64_t step;
+    int32_t type;
+    int16_t inter_type;
+    int16_t pad_;
+    double x[3];
+    double v[3];
+} orc_dump_record;
+int64_t orc_dump_records(const orc_sim *s, uint64_t time_step, orc_dump_record *out, int64_t cap);
+
 /* Time nsteps of the loop on this thread; returns wall seconds. */
 double orc_time_simulate(orc_sim *s, int64_t nsteps);
 

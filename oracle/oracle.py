@@ -22,6 +22,55 @@ ATOM_DTYPE = np.dtype(
 )
 
 
+# AtomInfoDump / the record tools/dump2text/out_convert.cpp:18-25 reads: 72 bytes on LP64
+DUMP_DTYPE = np.dtype(
+    [("id", "<u8"), ("step", "<u8"), ("type", "<i4"), ("inter_type", "<i2"), ("pad_", "<i2"),
+     ("x", "<f8", (3,)), ("v", "<f8", (3,))],
+    align=True,
+)
+DUMP_HEADER = 128        # HEADER_SIZE (out_convert.cpp:5)
+DUMP_RANK_HEADER = 128   # _LOCAL_HEADER_SIZE (out_convert.cpp:6)
+DUMP_BLOCK = 1024 * 72   # BLOCK_SIZE (out_convert.cpp:30): LocalStorage's block, 1024 records
+
+
+def write_dump_file(path, records):
+    """The copy-mode file of one rank (AtomDump::dump + writeDumpHeader, frontend/io/atom_dump.cpp:38-82,
+    through kiwi::LocalStorage): file header, rank header {size_t atoms_count}, then the records. With
+    one rank LocalStorage's blocks are consecutive, so the records are contiguous. The file header is
+    kiwi's and unread by any reader; it is written as zeros."""
+    records = np.ascontiguousarray(records, dtype=DUMP_DTYPE)
+    head = np.zeros(DUMP_HEADER + DUMP_RANK_HEADER, dtype=np.uint8)
+    head[DUMP_HEADER:DUMP_HEADER + 8] = np.frombuffer(np.uint64(records.size).tobytes(), dtype=np.uint8)
+    with open(path, "wb") as f:
+        f.write(head.tobytes())
+        f.write(records.tobytes())
+
+
+def read_dump_file(path, n_ranks=1):
+    """dump2text's reader (tools/dump2text/out_convert.cpp:66-98, readBytes :129-163) restated: for each
+    rank, its count from the rank header, then its records from its blocks, which LocalStorage
+    interleaves round-robin over the ranks. Returns one record array per rank."""
+    data = np.fromfile(path, dtype=np.uint8)
+    h = DUMP_HEADER + DUMP_RANK_HEADER * n_ranks
+    out = []
+    for rank in range(n_ranks):
+        at = DUMP_HEADER + DUMP_RANK_HEADER * rank
+        count = int(np.frombuffer(data[at:at + 8].tobytes(), dtype=np.uint64)[0])
+        want = count * DUMP_DTYPE.itemsize
+        parts, k = [], 0
+        while want > 0:  # block k of this rank starts at h + (n_ranks * k + rank) * BLOCK
+            lo = h + (n_ranks * k + rank) * DUMP_BLOCK
+            take = min(DUMP_BLOCK, want)
+            parts.append(data[lo:lo + take])
+            want -= take
+            k += 1
+        raw = np.concatenate(parts) if parts else np.zeros(0, dtype=np.uint8)
+        if raw.size != count * DUMP_DTYPE.itemsize:
+            raise ValueError(f"{path}: truncated (rank {rank}: {raw.size} bytes for {count} records)")
+        out.append(np.frombuffer(raw.tobytes(), dtype=DUMP_DTYPE))
+    return out
+
+
 class DomainDesc(ctypes.Structure):
     _fields_ = [("phase_space", ctypes.c_int64 * 3), ("lattice_const", ctypes.c_double),
                 ("cutoff_radius_factor", ctypes.c_double), ("grid_size", ctypes.c_int32 * 3),
@@ -75,6 +124,7 @@ _PROTOS = {
     "orc_collision_step": (None, [_P, _P, _P, _D]),
     "orc_setv": (None, [_P, _P, _P, _D]),
     "orc_world_build": (_I32, [_P, _D, ctypes.c_uint32, _P, _I32]),
+    "orc_dump_records": (_I64, [_P, _U64, _P, _I64]),
     "orc_mvv": (_D, [_P]),
     "orc_kinetic_energy": (_D, [_P]),
     "orc_temperature": (_D, [_P, _U64]),
@@ -258,6 +308,13 @@ class OracleSim:
         r = np.asarray(ratio, dtype=np.int32)
         if self.L.orc_world_build(self.h, float(t_set), int(seed), _ptr(r), int(rng)) != 0:
             raise ValueError("unknown random engine")
+
+    def dump_records(self, time_step):
+        n = self.L.orc_dump_records(self.h, int(time_step), None, 0)
+        out = np.zeros(n, dtype=DUMP_DTYPE)
+        if n:
+            self.L.orc_dump_records(self.h, int(time_step), _ptr(out), n)
+        return out
 
     def system_force(self):
         out = np.zeros(3)
