@@ -559,7 +559,8 @@ def run_ours(args):
                              "a second pass of the same steps with events around every kernel",
                    "parallelism": f"{world} independent replica(s), one per GPU"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io,
-                "path": "mg_step_host: pinned host slot array in, one loop body, slot array out"},
+                "path": "mg_step_host: pinned host slot array in, one loop body, slot array out; copies in 16 z-slabs "
+                        "overlapped with unpack/firststep (in) and the force pass (out)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic,
                      "kernel": "lat_force (mixed)", "kernel_ms": force_ms,

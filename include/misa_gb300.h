@@ -182,10 +182,17 @@ mg_status mg_clear_errors(mg_context *ctx);
 /* ---------------------------------------------------------------------------------------------
  * Drop-in full step with host state (the end-to-end path): uploads the host slot array and
  * inter-atom list, runs nsteps loop bodies on the GPU, downloads both back. The host arrays keep
- * being the state of record, as in the reference's host loop.
+ * being the state of record, as in the reference's host loop. Device errors of the step are
+ * returned (MG_ERR_CAPACITY, ...).
+ * One loop body with a fixed dt and no inter atoms in (*n_inter == 0) is pipelined: the slot array
+ * moves in z-slabs of whole planes, and each slab's copy overlaps the unpack and firststep of the
+ * previous one (in) or the force pass of the next one (out). The result is bit-identical to the
+ * unpipelined path. With a pinned slot array (mg_host_register) the copies run asynchronously.
  * ------------------------------------------------------------------------------------------- */
 mg_status mg_step_host(mg_context *ctx, mg_atom_element *atoms, int64_t n_slots, mg_atom_element *inter,
                        int64_t inter_cap, int64_t *n_inter, int64_t nsteps);
+/* Number of z-slabs of mg_step_host's pipeline (default 16; 0 or 1: no pipelining). */
+mg_status mg_set_host_pipeline(mg_context *ctx, int32_t chunks);
 
 /* ---------------------------------------------------------------------------------------------
  * Wigner-Seitz mapping on the GPU (src/lattice/ws_utils.cpp:91-189), for indexing parity checks:

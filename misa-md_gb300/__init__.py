@@ -123,6 +123,7 @@ _PROTOS = {
     "mg_dump_close": (_I32, [_P, _P]),
     "mg_dump_last_error": (ctypes.c_char_p, [_P]),
     "mg_set_stage_output": (_I32, [_P, _P, _U64, ctypes.c_char_p]),
+    "mg_set_host_pipeline": (_I32, [_P, _I32]),
 }
 
 
@@ -395,6 +396,10 @@ class Context:
 
     def eam_force_calc(self, atoms):
         self._check(self.lib.mg_eam_force_calc(self.h, _ptr(atoms), self.cutoff_radius))
+
+    def set_host_pipeline(self, chunks):
+        """z-slabs of step_host's copy/compute pipeline (0 or 1: off)."""
+        self._check(self.lib.mg_set_host_pipeline(self.h, int(chunks)))
 
     def step_host(self, atoms, inter, n_inter, nsteps):
         n = ctypes.c_int64(n_inter)

@@ -78,6 +78,10 @@ struct mg_context {
     std::vector<double> timer_ms;      // accumulated per kernel
     int64_t timed_steps = 0;
     bool energy_valid = false;
+    // mg_step_host pipeline: z-slab chunks (< 2: off), its copy streams and events
+    int host_chunks = 16;
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    std::vector<cudaEvent_t> pipe_ev;
     // stage-machine dumps (mg_set_stage_output)
     mg_dump *stage_dump = nullptr;
     uint64_t stage_dump_interval = 0;
@@ -159,12 +163,13 @@ struct Timer {
 // ---- the kernel sequences ----
 void seq_firststep(mg_context *ctx, bool decide, Timer *t) {
     const LaunchCtx lc = ctx->lc();
-    launch_firststep(lc, ctx->g, ctx->s, ctx->in, ctx->d_sp, decide, ctx->mixed());
+    launch_firststep(lc, ctx->g, ctx->s, ctx->in, ctx->d_sp, decide);
     if (t) t->mark(1);
     launch_inter_firststep(lc, ctx->in, ctx->d_sp);
     if (t) t->mark(2);
 }
-void seq_compute_eam(mg_context *ctx, bool kick, bool with_manage_prefix, int manage_mask, Timer *t) {
+// computeEam up to the forward df exchange: list work, ghost copy, rho, dF/drho, ghost df
+void seq_eam_density(mg_context *ctx, bool with_manage_prefix, int manage_mask, Timer *t) {
     const LaunchCtx lc = ctx->lc();
     const bool mx = ctx->mixed();
     const bool decide = with_manage_prefix && (manage_mask & MANAGE_DECIDE);
@@ -186,12 +191,20 @@ void seq_compute_eam(mg_context *ctx, bool kick, bool with_manage_prefix, int ma
     if (t) t->mark(7);
     launch_ghost_df(lc, ctx->g, ctx->s, ctx->in, mx);
     if (t) t->mark(8);
-    launch_lat_force(lc, ctx->g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, kick, mx, false);
-    if (t) t->mark(9);
-    launch_inter_force(lc, ctx->g, ctx->s, ctx->in, ctx->pt, mx);
+}
+// the inter-atom force pass and the second half-kick, after the lattice force pass
+void seq_eam_force_tail(mg_context *ctx, bool kick, Timer *t) {
+    const LaunchCtx lc = ctx->lc();
+    launch_inter_force(lc, ctx->g, ctx->s, ctx->in, ctx->pt, ctx->mixed());
     if (t) t->mark(10);
     if (kick) launch_secondstep(lc, ctx->g, ctx->s, ctx->in, ctx->d_sp, false);
     if (t) t->mark(11);
+}
+void seq_compute_eam(mg_context *ctx, bool kick, bool with_manage_prefix, int manage_mask, Timer *t) {
+    seq_eam_density(ctx, with_manage_prefix, manage_mask, t);
+    launch_lat_force(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, kick, ctx->mixed(), false);
+    if (t) t->mark(9);
+    seq_eam_force_tail(ctx, kick, t);
 }
 // one loop body: firststep, decide, exchangeInter, borderInter, exchangeAtom, computeEam, secondstep
 void seq_step(mg_context *ctx, Timer *t) {
@@ -536,6 +549,9 @@ mg_status mg_destroy(mg_context *ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     for (cudaEvent_t e : ctx->ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->pipe_ev) cudaEventDestroy(e);
+    if (ctx->copy_in) cudaStreamDestroy(ctx->copy_in);
+    if (ctx->copy_out) cudaStreamDestroy(ctx->copy_out);
     for (void *p : ctx->dev_allocs) cudaFree(p);
     if (ctx->pot_mem) cudaFree(ctx->pot_mem);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1128,9 +1144,109 @@ mg_status mg_clear_errors(mg_context *ctx) {
     return MG_OK;
 }
 
+// One loop body from and to the host slot array with the copies overlapped by the step (fixed dt, no
+// inter atoms in). The slot grid is cut into z-slabs of whole planes:
+//   in:  slab c is copied in on copy_in while slab c - 1 is unpacked and takes its firststep;
+//   out: the force pass runs slab by slab; once a slab's planes are final they are packed and copied out
+//        on copy_out while the next slab computes (the ghost planes below the box right after ghost df).
+// Per atom the kernels and their order are those of mg_upload + mg_simulate + mg_download, so the
+// result is bit-identical. If decide moved atoms off the lattice this step, the inter-atom passes
+// changed forces after the slabs went out: the whole state is then downloaded again.
+static mg_status step_host_pipelined(mg_context *ctx, mg_atom_element *atoms, mg_atom_element *inter, int64_t inter_cap,
+                                     int64_t *n_inter) {
+    const Geom &g = ctx->g;
+    const int S = std::min(ctx->host_chunks, g.bz);
+    if (!ctx->copy_in) MG_CK(cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
+    if (!ctx->copy_out) MG_CK(cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));
+    const size_t n_ev = static_cast<size_t>(2 * S + 4);
+    while (ctx->pipe_ev.size() < n_ev) {
+        cudaEvent_t e;
+        MG_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->pipe_ev.push_back(e);
+    }
+    mg_status st;
+    if ((st = ensure_aos(ctx)) != MG_OK) return st;
+    const LaunchCtx lc = ctx->lc();
+    const bool mx = ctx->mixed();
+    const int64_t plane = static_cast<int64_t>(g.Sx) * g.Sy;  // slots per z plane
+    const size_t rec = sizeof(mg_atom_element);
+    size_t ev = 0;
+    auto local_plane_bound = [&](int c) { return static_cast<int>((static_cast<int64_t>(c) * g.bz) / S); };
+
+    // in: the copies wait for everything already on the library stream
+    MG_CK(cudaEventRecord(ctx->pipe_ev[ev], ctx->stream));
+    MG_CK(cudaStreamWaitEvent(ctx->copy_in, ctx->pipe_ev[ev++], 0));
+    launch_set_counts(lc, ctx->in, 0);
+    launch_step_head(lc, ctx->d_sp);
+    for (int c = 0; c < S; c++) {
+        const int z0 = c == 0 ? 0 : g.gz + local_plane_bound(c);
+        const int z1 = c == S - 1 ? g.Sz : g.gz + local_plane_bound(c + 1);
+        const int64_t s0 = z0 * plane, s1 = z1 * plane;
+        MG_CK(cudaMemcpyAsync(ctx->d_aos + s0, atoms + s0, static_cast<size_t>(s1 - s0) * rec, cudaMemcpyHostToDevice,
+                              ctx->copy_in));
+        MG_CK(cudaEventRecord(ctx->pipe_ev[ev], ctx->copy_in));
+        MG_CK(cudaStreamWaitEvent(ctx->stream, ctx->pipe_ev[ev++], 0));
+        launch_unpack_aos(lc, g, ctx->d_aos, ctx->s, ctx->in, ctx->types_ok_mask, mx, static_cast<int>(s0),
+                          static_cast<int>(s1));
+        const int k0 = std::max(z0 - g.gz, 0), k1 = std::min(z1 - g.gz, g.bz);
+        if (k1 > k0) launch_firststep(lc, g, ctx->s, ctx->in, ctx->d_sp, true, k0 * g.by * g.bx, k1 * g.by * g.bx);
+    }
+    launch_inter_firststep(lc, ctx->in, ctx->d_sp);
+    seq_eam_density(ctx, true, MANAGE_DECIDE | MANAGE_CLEAR_GHOST | MANAGE_EXCHANGE | MANAGE_BORDER, nullptr);
+
+    // out: pack the planes [z0, z1) once final and copy them on copy_out
+    auto flush = [&](int z0, int z1) -> mg_status {
+        if (z1 <= z0) return MG_OK;
+        const int64_t s0 = z0 * plane, s1 = z1 * plane;
+        launch_pack_aos(lc, g, ctx->d_aos, ctx->s, PACK_ALL, mx, static_cast<int>(s0), static_cast<int>(s1));
+        MG_CK(cudaEventRecord(ctx->pipe_ev[ev], ctx->stream));
+        MG_CK(cudaStreamWaitEvent(ctx->copy_out, ctx->pipe_ev[ev++], 0));
+        MG_CK(cudaMemcpyAsync(atoms + s0, ctx->d_aos + s0, static_cast<size_t>(s1 - s0) * rec, cudaMemcpyDeviceToHost,
+                              ctx->copy_out));
+        return MG_OK;
+    };
+    if ((st = flush(0, g.gz)) != MG_OK) return st;
+    const int64_t per_plane = static_cast<int64_t>(g.by) * g.nxh;  // sites of one parity per local plane
+    int u0 = 0, z_done = g.gz;
+    for (int c = 0; c < S; c++) {
+        const bool last = c == S - 1;
+        const int u1 = last ? g.n_local_half : static_cast<int>(((local_plane_bound(c + 1) * per_plane) >> 5) << 5);
+        launch_lat_force_sites(lc, g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, true, mx, u0, u1);
+        const int z_to = last ? g.Sz : g.gz + static_cast<int>(u1 / per_plane);
+        if ((st = flush(z_done, z_to)) != MG_OK) return st;
+        z_done = std::max(z_done, z_to);
+        u0 = u1;
+    }
+    seq_eam_force_tail(ctx, true, nullptr);
+    if ((st = check_launch(ctx)) != MG_OK) return st;
+
+    int cnt[CNT_WORDS];
+    MG_CK(cudaMemcpyAsync(cnt, ctx->in.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_CK(cudaStreamSynchronize(ctx->stream));
+    MG_CK(cudaStreamSynchronize(ctx->copy_out));
+    ctx->prepared = true;
+    ctx->vmax_stale = true;
+    ctx->energy_valid = false;
+    if (cnt[CNT_INTER] > 0) {
+        if ((st = mg_download(ctx, atoms, g.n_slots, inter, inter_cap, n_inter)) != MG_OK) return st;
+    } else {
+        *n_inter = 0;
+    }
+    return status_from_bits(ctx, static_cast<uint32_t>(cnt[CNT_ERRORS]));
+}
+
+mg_status mg_set_host_pipeline(mg_context *ctx, int32_t chunks) {
+    if (!ctx || chunks < 0) return MG_ERR_ARG;
+    ctx->host_chunks = chunks;
+    return MG_OK;
+}
+
 mg_status mg_step_host(mg_context *ctx, mg_atom_element *atoms, int64_t n_slots, mg_atom_element *inter,
                        int64_t inter_cap, int64_t *n_inter, int64_t nsteps) {
     if (!ctx || !atoms || !n_inter) return MG_ERR_ARG;
+    if (nsteps == 1 && *n_inter == 0 && n_slots == ctx->g.n_slots && ctx->host_chunks >= 2 && ctx->dx_max <= 0.0 &&
+        !ctx->timing && ctx->pot_ready)
+        return step_host_pipelined(ctx, atoms, inter, inter_cap, n_inter);
     mg_status st = mg_upload(ctx, atoms, n_slots, inter, std::min<int64_t>(*n_inter, inter_cap));
     if (st != MG_OK) return st;
     ctx->prepared = true;  // the host state carries forces from its previous computeEam

@@ -212,14 +212,18 @@ struct LaunchCtx {
 // Mass table shared by all contexts (atom types are fixed).
 void set_mass_table(cudaStream_t stream);
 
+// AoS <-> SoA over the slots [s0, s1) (s1 < 0: to the end of the grid)
 void launch_unpack_aos(const LaunchCtx &lc, const Geom &g, const mg_atom_element *aos, Slots s, Inter in, int types_ok_mask,
-                       bool mixed);
+                       bool mixed, int s0 = 0, int s1 = -1);
 // set CNT_INTER = n_inter and clear the ghost and displaced counts
 void launch_set_counts(const LaunchCtx &lc, Inter in, int n_inter);
-void launch_pack_aos(const LaunchCtx &lc, const Geom &g, mg_atom_element *aos, Slots s, int fields, bool mixed);
+void launch_pack_aos(const LaunchCtx &lc, const Geom &g, mg_atom_element *aos, Slots s, int fields, bool mixed,
+                     int s0 = 0, int s1 = -1);
 enum { PACK_ALL = 0xff, PACK_RHO = 1, PACK_DF = 2, PACK_F = 4 };
 
-void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const StepParams *sp, bool decide, bool mixed);
+// local atoms [t0, t1) in k, j, i order (t1 < 0: all)
+void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const StepParams *sp, bool decide, int t0 = 0,
+                      int t1 = -1);
 // fill g.site_half (once per context)
 void launch_site_table(const LaunchCtx &lc, const Geom &g, double *site_half);
 void launch_decide_scan(const LaunchCtx &lc, const Geom &g, Slots s, Inter in);
@@ -234,6 +238,10 @@ void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTa
 void launch_lat_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook);
 void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *sp, bool kick,
                       bool mixed, bool hook);
+// the force pass over the sites of both parities whose index within their parity is in [u0, u1):
+// with u0 and u1 multiples of 32 (or u1 = n_local_half) the slabs of a split pass are disjoint warps
+void launch_lat_force_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *sp, bool kick,
+                            bool mixed, int u0, int u1);
 void launch_secondstep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams *sp, bool lattice);
 // step head: records the step's dt and, in variable mode, sets dt from the last kick's max |v|
 void launch_step_head(const LaunchCtx &lc, StepParams *sp);

@@ -284,9 +284,10 @@ __device__ __forceinline__ void kahan(float &sum, float &comp, float term) {
 // ------------------------------------------------------------------------------------------------
 // AoS <-> SoA (the reference's AtomElement array crosses the boundary as raw records)
 // ------------------------------------------------------------------------------------------------
-__global__ void k_unpack_aos(Geom g, const mg_atom_element *aos, Slots s, Inter in, int types_ok_mask, bool mixed) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.n_slots) return;
+__global__ void k_unpack_aos(Geom g, const mg_atom_element *aos, Slots s, Inter in, int types_ok_mask, bool mixed, int s0,
+                             int s1) {
+    const int t = s0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= s1) return;
     mg_atom_element a = aos[t];
     if (a.type < -1 || a.type > 2 || (a.type >= 0 && !((types_ok_mask >> a.type) & 1))) {
         set_error(in, MG_DEVERR_BAD_TYPE);
@@ -307,9 +308,9 @@ __global__ void k_unpack_aos(Geom g, const mg_atom_element *aos, Slots s, Inter 
     if (mixed) s.df32[sidx(g, t)] = (float) a.df;
 }
 
-__global__ void k_pack_aos(Geom g, mg_atom_element *aos, Slots s, int fields, bool mixed) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.n_slots) return;
+__global__ void k_pack_aos(Geom g, mg_atom_element *aos, Slots s, int fields, bool mixed, int s0, int s1) {
+    const int t = s0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= s1) return;
     mg_atom_element &a = aos[t];
     const double df = mixed ? (double) s.df32[sidx(g, t)] : s.df[t];
     if (fields == PACK_ALL) {
@@ -331,9 +332,11 @@ __global__ void k_pack_aos(Geom g, mg_atom_element *aos, Slots s, int fields, bo
 }
 
 void launch_unpack_aos(const LaunchCtx &lc, const Geom &g, const mg_atom_element *aos, Slots s, Inter in,
-                       int types_ok_mask, bool mixed) {
+                       int types_ok_mask, bool mixed, int s0, int s1) {
+    if (s1 < 0) s1 = g.n_slots;
+    if (s1 <= s0) return;
     const int b = 256;
-    k_unpack_aos<<<(g.n_slots + b - 1) / b, b, 0, lc.stream>>>(g, aos, s, in, types_ok_mask, mixed);
+    k_unpack_aos<<<(s1 - s0 + b - 1) / b, b, 0, lc.stream>>>(g, aos, s, in, types_ok_mask, mixed, s0, s1);
 }
 __global__ void k_set_counts(Inter in, int n_inter) {
     in.cnt[CNT_INTER] = n_inter;
@@ -343,9 +346,12 @@ __global__ void k_set_counts(Inter in, int n_inter) {
     *in.n_bucket = 0;
 }
 void launch_set_counts(const LaunchCtx &lc, Inter in, int n_inter) { k_set_counts<<<1, 1, 0, lc.stream>>>(in, n_inter); }
-void launch_pack_aos(const LaunchCtx &lc, const Geom &g, mg_atom_element *aos, Slots s, int fields, bool mixed) {
+void launch_pack_aos(const LaunchCtx &lc, const Geom &g, mg_atom_element *aos, Slots s, int fields, bool mixed, int s0,
+                     int s1) {
+    if (s1 < 0) s1 = g.n_slots;
+    if (s1 <= s0) return;
     const int b = 256;
-    k_pack_aos<<<(g.n_slots + b - 1) / b, b, 0, lc.stream>>>(g, aos, s, fields, mixed);
+    k_pack_aos<<<(s1 - s0 + b - 1) / b, b, 0, lc.stream>>>(g, aos, s, fields, mixed, s0, s1);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -377,9 +383,10 @@ __device__ __noinline__ bool exact_displaced(double ex, double ey, double ez, do
 }
 
 template <bool MOVE, bool DECIDE>
-__global__ void __launch_bounds__(kFirstThreads) k_firststep(Geom g, Slots s, Inter in, const StepParams *__restrict__ p) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.n_local) return;
+__global__ void __launch_bounds__(kFirstThreads) k_firststep(Geom g, Slots s, Inter in, const StepParams *__restrict__ p,
+                                                             int t0, int t1) {
+    const int t = t0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= t1) return;
     int i, j, k;
     const int sl = local_slot(g, t, i, j, k);
     const int ty = s.type[sl];
@@ -505,14 +512,17 @@ __global__ void k_disp_collect(Geom g, Inter in, int nblocks) {
     }
 }
 
-void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const StepParams *p, bool decide, bool) {
-    const int b = kFirstThreads, n = (g.n_local + b - 1) / b;
-    if (decide) k_firststep<true, true><<<n, b, 0, lc.stream>>>(g, s, in, p);
-    else k_firststep<true, false><<<n, b, 0, lc.stream>>>(g, s, in, p);
+void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const StepParams *p, bool decide, int t0,
+                      int t1) {
+    if (t1 < 0) t1 = g.n_local;
+    if (t1 <= t0) return;
+    const int b = kFirstThreads, n = (t1 - t0 + b - 1) / b;
+    if (decide) k_firststep<true, true><<<n, b, 0, lc.stream>>>(g, s, in, p, t0, t1);
+    else k_firststep<true, false><<<n, b, 0, lc.stream>>>(g, s, in, p, t0, t1);
 }
 void launch_decide_scan(const LaunchCtx &lc, const Geom &g, Slots s, Inter in) {
     const int b = kFirstThreads, n = (g.n_local + b - 1) / b;
-    k_firststep<false, true><<<n, b, 0, lc.stream>>>(g, s, in, nullptr);
+    k_firststep<false, true><<<n, b, 0, lc.stream>>>(g, s, in, nullptr, 0, g.n_local);
 }
 void launch_displaced_collect(const LaunchCtx &lc, const Geom &g, Inter in) {
     const int nblocks = (g.n_local + kFirstThreads - 1) / kFirstThreads;
@@ -864,8 +874,9 @@ __device__ __forceinline__ void k_lat_force_fp64_site(int t, const NeighTables &
 }
 template <bool LOOP>  // LOOP: several sites per thread, one grid stride apart
 __global__ void __launch_bounds__(512) k_lat_force_fp64(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt,
-                                                         StepParams *sp, bool kick, bool hook, int order, int nthreads) {
-    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+                                                         StepParams *sp, bool kick, bool hook, int order, int tbase,
+                                                         int nthreads) {
+    const int t0 = tbase + blockIdx.x * blockDim.x + threadIdx.x;  // threads [tbase, nthreads)
     if (!LOOP) {
         if (t0 < nthreads) k_lat_force_fp64_site(t0, nt, g, s, in, pt, sp, kick, hook, order);
         return;
@@ -957,8 +968,9 @@ __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables 
 }
 template <bool LOOP>  // LOOP: several sites per thread, one grid stride apart
 __global__ void __launch_bounds__(512, 3) k_lat_force_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt,
-                                                         StepParams *sp, bool kick, bool hook, int order, int nthreads) {
-    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+                                                         StepParams *sp, bool kick, bool hook, int order, int tbase,
+                                                         int nthreads) {
+    const int t0 = tbase + blockIdx.x * blockDim.x + threadIdx.x;  // threads [tbase, nthreads)
     if (!LOOP) {
         if (t0 < nthreads) k_lat_force_mixed_site(t0, nt, g, s, in, pt, sp, kick, hook, order);
         return;
@@ -966,16 +978,33 @@ __global__ void __launch_bounds__(512, 3) k_lat_force_mixed(const __grid_constan
     for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x) k_lat_force_mixed_site(t, nt, g, s, in, pt, sp, kick, hook, order);
 }
 
+static void launch_lat_force_threads(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *p,
+                                     bool kick, bool mixed, bool hook, int tb, int te) {
+    const int order = lc.force_order, b = lc.force_block;
+    const int n = (te - tb + b * lc.force_apt - 1) / (b * lc.force_apt);
+    if (n <= 0) return;
+    if (lc.force_apt > 1) {
+        if (mixed) k_lat_force_mixed<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te);
+        else k_lat_force_fp64<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te);
+    } else {
+        if (mixed) k_lat_force_mixed<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te);
+        else k_lat_force_fp64<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te);
+    }
+}
 void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *p, bool kick,
                       bool mixed, bool hook) {
-    const int order = lc.force_order, b = lc.force_block, nthr = gather_threads(g, order);
-    const int n = (nthr + b * lc.force_apt - 1) / (b * lc.force_apt);
-    if (lc.force_apt > 1) {
-        if (mixed) k_lat_force_mixed<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, nthr);
-        else k_lat_force_fp64<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, nthr);
-    } else {
-        if (mixed) k_lat_force_mixed<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, nthr);
-        else k_lat_force_fp64<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, nthr);
+    launch_lat_force_threads(lc, g, s, in, t, p, kick, mixed, hook, 0, gather_threads(g, lc.force_order));
+}
+void launch_lat_force_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *p, bool kick,
+                            bool mixed, int u0, int u1) {
+    if (u1 <= u0) return;
+    if (lc.force_order) {  // warp w of parity p covers sites 32 (w / 2) .. + 31: thread t = 64 (u / 32) + 32 p + u % 32
+        const int tb = (u0 >> 5) << 6;
+        const int te = u1 >= g.n_local_half ? gather_threads(g, 1) : (u1 >> 5) << 6;
+        launch_lat_force_threads(lc, g, s, in, t, p, kick, mixed, false, tb, te);
+    } else {               // parity-major threads: one launch per parity
+        launch_lat_force_threads(lc, g, s, in, t, p, kick, mixed, false, u0, u1);
+        launch_lat_force_threads(lc, g, s, in, t, p, kick, mixed, false, g.n_local_half + u0, g.n_local_half + u1);
     }
 }
 

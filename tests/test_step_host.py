@@ -1,0 +1,101 @@
+"""mg_step_host: the pipelined path (slot array moved in z-slabs, copies overlapped with firststep and
+the force pass) against the unpipelined path (mg_upload + mg_simulate + mg_download), bit for bit, and
+against the CPU oracle. Covers both precisions, several chained calls, slab counts that do not divide
+the box, and a step whose decide moves an atom off the lattice (the pipeline's fallback download)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+A0 = 2.855
+RCF = 5.6 / A0
+
+
+def _ctx(pkg, cells, pot, precision, chunks):
+    c = pkg.Context(cells, A0, RCF, precision=precision, inter_capacity=1024)
+    c.pot_init_setfl(pot)
+    c.set_timestep(0.001)
+    c.set_host_pipeline(chunks)
+    return c
+
+
+def _prepared_state(pkg, wl, cells, pot, precision, alloy=True):
+    """A state whose forces come from a computeEam (as the reference host state does after a step)."""
+    c = _ctx(pkg, cells, pot, precision, 0)
+    c.upload(wl.build_state(cells, A0, RCF, temperature=600.0, seed=9, cu_frac=0.05 if alloy else 0.0,
+                            ni_frac=0.03 if alloy else 0.0))
+    c.prepare()
+    a, inter = c.download()
+    c.close()
+    return a, inter
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("chunks", [2, 5, 8])
+def test_pipelined_step_host_is_bit_identical(pkg, wl, potentials, gpu_lib, precision, chunks):
+    cells = (11, 9, 13)
+    a0, _ = _prepared_state(pkg, wl, cells, potentials["fecuni"], precision)
+    got, want = a0.copy(), a0.copy()
+    cp = _ctx(pkg, cells, potentials["fecuni"], precision, chunks)
+    cu = _ctx(pkg, cells, potentials["fecuni"], precision, 0)
+    inter_p = np.zeros(64, dtype=pkg.ATOM_DTYPE)
+    inter_u = np.zeros(64, dtype=pkg.ATOM_DTYPE)
+    np_, nu = 0, 0
+    for _ in range(4):
+        np_ = cp.step_host(got, inter_p, np_, 1)
+        nu = cu.step_host(want, inter_u, nu, 1)
+        assert np_ == nu == 0
+        assert got.tobytes() == want.tobytes()
+    cp.close()
+    cu.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_pipelined_step_host_falls_back_when_decide_moves_atoms(pkg, wl, potentials, gpu_lib, precision):
+    """An atom moved 0.3 a0 along (1, 1, 1), so that its nearest site is an occupied neighbour's,
+    becomes an inter atom in the step's decide and stays one (an atom nearest its own vacated site
+    would recombine into it at once). The pipeline then downloads the whole state again, and the
+    result still equals the unpipelined path."""
+    cells = (10, 10, 10)
+    a0, _ = _prepared_state(pkg, wl, cells, potentials["fecuni"], precision)
+    loc = wl.local_slot_indices(cells, RCF)
+    a0["x"][loc[1234]] += 0.3 * A0 * np.ones(3)
+    got, want = a0.copy(), a0.copy()
+    cp = _ctx(pkg, cells, potentials["fecuni"], precision, 8)
+    cu = _ctx(pkg, cells, potentials["fecuni"], precision, 0)
+    inter_p = np.zeros(64, dtype=pkg.ATOM_DTYPE)
+    inter_u = np.zeros(64, dtype=pkg.ATOM_DTYPE)
+    np_ = cp.step_host(got, inter_p, 0, 1)
+    nu = cu.step_host(want, inter_u, 0, 1)
+    assert np_ == nu == 1
+    assert got.tobytes() == want.tobytes()
+    assert inter_p[:1].tobytes() == inter_u[:1].tobytes()
+    assert got["type"][loc[1234]] == -1
+    # the next call has an inter atom in, so it takes the unpipelined path on both contexts
+    np_ = cp.step_host(got, inter_p, np_, 1)
+    nu = cu.step_host(want, inter_u, nu, 1)
+    assert np_ == nu and got.tobytes() == want.tobytes()
+    cp.close()
+    cu.close()
+
+
+def test_pipelined_step_host_matches_oracle(pkg, orc, wl, potentials, gpu_lib):
+    """Three pipelined FP64 calls against three oracle loop bodies from the same host state."""
+    cells = (9, 9, 9)
+    a0, _ = _prepared_state(pkg, wl, cells, potentials["fe"], "fp64", alloy=False)
+    got = a0.copy()
+    cp = _ctx(pkg, cells, potentials["fe"], "fp64", 4)
+    inter = np.zeros(16, dtype=pkg.ATOM_DTYPE)
+    n = 0
+    for _ in range(3):
+        n = cp.step_host(got, inter, n, 1)
+    ref = orc.OracleSim(cells, A0, RCF, potentials["fe"], dt=0.001)
+    ref.set_atoms(a0)
+    ref.exchange_atom_first()
+    ref.simulate(3)
+    w = ref.get_atoms()
+    loc = wl.local_slot_indices(cells, RCF)
+    assert np.array_equal(got["type"][loc], w["type"][loc]) and np.array_equal(got["id"][loc], w["id"][loc])
+    assert np.abs(got["x"][loc] - w["x"][loc]).max() < 1e-12
+    assert np.abs(got["f"][loc] - w["f"][loc]).max() < 1e-9
+    cp.close()
