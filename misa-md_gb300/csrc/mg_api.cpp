@@ -168,8 +168,8 @@ void seq_firststep(mg_context *ctx, bool decide, Timer *t) {
     launch_inter_firststep(lc, ctx->in, ctx->d_sp);
     if (t) t->mark(2);
 }
-// computeEam up to the forward df exchange: list work, ghost copy, rho, dF/drho, ghost df
-void seq_eam_density(mg_context *ctx, bool with_manage_prefix, int manage_mask, Timer *t) {
+// computeEam's list work (decide, exchangeInter, borderInter, makeIndex) and the lattice ghost copy
+void seq_eam_lists(mg_context *ctx, bool with_manage_prefix, int manage_mask, Timer *t) {
     const LaunchCtx lc = ctx->lc();
     const bool mx = ctx->mixed();
     const bool decide = with_manage_prefix && (manage_mask & MANAGE_DECIDE);
@@ -183,6 +183,11 @@ void seq_eam_density(mg_context *ctx, bool with_manage_prefix, int manage_mask, 
     if (t) t->mark(3);
     launch_ghost_copy(lc, ctx->g, ctx->s, mx);
     if (t) t->mark(4);
+}
+// rho, dF/drho and the forward df exchange
+void seq_eam_rho(mg_context *ctx, Timer *t) {
+    const LaunchCtx lc = ctx->lc();
+    const bool mx = ctx->mixed();
     launch_lat_rho(lc, ctx->g, ctx->s, ctx->in, ctx->pt, mx, false);
     if (t) t->mark(5);
     launch_inter_rho(lc, ctx->g, ctx->s, ctx->in, ctx->pt, mx);
@@ -201,7 +206,8 @@ void seq_eam_force_tail(mg_context *ctx, bool kick, Timer *t) {
     if (t) t->mark(11);
 }
 void seq_compute_eam(mg_context *ctx, bool kick, bool with_manage_prefix, int manage_mask, Timer *t) {
-    seq_eam_density(ctx, with_manage_prefix, manage_mask, t);
+    seq_eam_lists(ctx, with_manage_prefix, manage_mask, t);
+    seq_eam_rho(ctx, t);
     launch_lat_force(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, kick, ctx->mixed(), false);
     if (t) t->mark(9);
     seq_eam_force_tail(ctx, kick, t);
@@ -1147,11 +1153,12 @@ mg_status mg_clear_errors(mg_context *ctx) {
 // One loop body from and to the host slot array with the copies overlapped by the step (fixed dt, no
 // inter atoms in). The slot grid is cut into z-slabs of whole planes:
 //   in:  slab c is copied in on copy_in while slab c - 1 is unpacked and takes its firststep;
-//   out: the force pass runs slab by slab; once a slab's planes are final they are packed and copied out
-//        on copy_out while the next slab computes (the ghost planes below the box right after ghost df).
-// Per atom the kernels and their order are those of mg_upload + mg_simulate + mg_download, so the
-// result is bit-identical. If decide moved atoms off the lattice this step, the inter-atom passes
-// changed forces after the slabs went out: the whole state is then downloaded again.
+//   out: density and force run slab by slab; once a slab's planes are final they are packed and copied
+//        out on copy_out while the next slabs compute.
+// Per atom the kernels are those of mg_upload + mg_simulate + mg_download, so the result is
+// bit-identical. The host reads the inter-atom count after decide: if decide moved atoms off the
+// lattice, their density and force passes follow the lattice passes, so the step finishes unsplit
+// and the state goes out in one download.
 static mg_status step_host_pipelined(mg_context *ctx, mg_atom_element *atoms, mg_atom_element *inter, int64_t inter_cap,
                                      int64_t *n_inter) {
     const Geom &g = ctx->g;
@@ -1192,7 +1199,26 @@ static mg_status step_host_pipelined(mg_context *ctx, mg_atom_element *atoms, mg
         if (k1 > k0) launch_firststep(lc, g, ctx->s, ctx->in, ctx->d_sp, true, k0 * g.by * g.bx, k1 * g.by * g.bx);
     }
     launch_inter_firststep(lc, ctx->in, ctx->d_sp);
-    seq_eam_density(ctx, true, MANAGE_DECIDE | MANAGE_CLEAR_GHOST | MANAGE_EXCHANGE | MANAGE_BORDER, nullptr);
+    seq_eam_lists(ctx, true, MANAGE_DECIDE | MANAGE_CLEAR_GHOST | MANAGE_EXCHANGE | MANAGE_BORDER, nullptr);
+    // whether decide left inter atoms: they add density and force after the lattice passes, which
+    // orders the whole density pass before any force (and the slabs' early copies would be stale)
+    int n_inter_now = 0;
+    MG_CK(cudaMemcpyAsync(&n_inter_now, ctx->in.cnt + CNT_INTER, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_CK(cudaStreamSynchronize(ctx->stream));
+    if ((st = check_launch(ctx)) != MG_OK) return st;
+    if (n_inter_now > 0) {  // the unpipelined remainder, then one download of everything
+        seq_eam_rho(ctx, nullptr);
+        launch_lat_force(lc, g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, true, mx, false);
+        seq_eam_force_tail(ctx, true, nullptr);
+        if ((st = check_launch(ctx)) != MG_OK) return st;
+        ctx->prepared = true;
+        ctx->vmax_stale = true;
+        ctx->energy_valid = false;
+        if ((st = mg_download(ctx, atoms, g.n_slots, inter, inter_cap, n_inter)) != MG_OK) return st;
+        uint32_t bits = 0;
+        if ((st = read_device_errors(ctx, &bits)) != MG_OK) return st;
+        return status_from_bits(ctx, bits);
+    }
 
     // out: pack the planes [z0, z1) once final and copy them on copy_out
     auto flush = [&](int z0, int z1) -> mg_status {
@@ -1205,17 +1231,49 @@ static mg_status step_host_pipelined(mg_context *ctx, mg_atom_element *atoms, mg
                               ctx->copy_out));
         return MG_OK;
     };
-    if ((st = flush(0, g.gz)) != MG_OK) return st;
+    // Density and force in S z-slabs of sites. A site's neighbours lie within 3 planes, so with slabs of
+    // at least 4 planes the force of slab c needs the density of slabs c - 1 .. c + 1 only, and the
+    // ghost planes (periodic images of the top and bottom slabs) only for slabs 0 and S - 1. Order:
+    // rho 0, rho 1, then per c = 1 .. S - 2 rho c + 1 and force c (its planes go out), then the ghost
+    // planes' df, force S - 1 and force 0. Without inter atoms every site's df is final after its
+    // density slab (dF/drho is fused), and the in-plane ghosts' df after that plane's density.
     const int64_t per_plane = static_cast<int64_t>(g.by) * g.nxh;  // sites of one parity per local plane
-    int u0 = 0, z_done = g.gz;
-    for (int c = 0; c < S; c++) {
-        const bool last = c == S - 1;
-        const int u1 = last ? g.n_local_half : static_cast<int>(((local_plane_bound(c + 1) * per_plane) >> 5) << 5);
-        launch_lat_force_sites(lc, g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, true, mx, u0, u1);
-        const int z_to = last ? g.Sz : g.gz + static_cast<int>(u1 / per_plane);
-        if ((st = flush(z_done, z_to)) != MG_OK) return st;
-        z_done = std::max(z_done, z_to);
-        u0 = u1;
+    const int SS = std::min(S, g.bz / 4);
+    if (SS < 3) {
+        seq_eam_rho(ctx, nullptr);
+        if ((st = flush(0, g.gz)) != MG_OK) return st;
+        launch_lat_force(lc, g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, true, mx, false);
+        if ((st = flush(g.gz, g.Sz)) != MG_OK) return st;
+    } else {
+        std::vector<int> u(SS + 1);
+        for (int c = 0; c <= SS; c++)
+            u[c] = c == SS ? g.n_local_half
+                           : static_cast<int>((((static_cast<int64_t>(c) * g.bz / SS) * per_plane) >> 5) << 5);
+        auto full_planes = [&](int c) { return c == SS ? g.bz : static_cast<int>(u[c] / per_plane); };  // below u[c]
+        int df_done = 0;  // local planes whose in-plane ghosts have their df
+        auto rho_slab = [&](int c) {
+            launch_lat_rho_sites(lc, g, ctx->s, ctx->in, ctx->pt, mx, u[c], u[c + 1]);
+            const int k = full_planes(c + 1);
+            launch_ghost_df_planes(lc, g, ctx->s, ctx->in, mx, df_done, k);
+            df_done = k;
+        };
+        rho_slab(0);
+        rho_slab(1);
+        // planes of slabs 1 .. S - 2 go out after their force; the plane cut by u[1] waits for slab 0
+        int z_done = g.gz + (u[1] % per_plane ? full_planes(1) + 1 : full_planes(1));
+        const int z_first = z_done;
+        for (int c = 1; c <= SS - 2; c++) {
+            rho_slab(c + 1);
+            launch_lat_force_sites(lc, g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, true, mx, u[c], u[c + 1]);
+            const int z_to = g.gz + full_planes(c + 1);
+            if ((st = flush(z_done, z_to)) != MG_OK) return st;
+            z_done = std::max(z_done, z_to);
+        }
+        launch_ghost_df_planes(lc, g, ctx->s, ctx->in, mx, -1, -1);
+        launch_lat_force_sites(lc, g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, true, mx, u[SS - 1], u[SS]);
+        if ((st = flush(z_done, g.Sz)) != MG_OK) return st;
+        launch_lat_force_sites(lc, g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, true, mx, u[0], u[1]);
+        if ((st = flush(0, z_first)) != MG_OK) return st;
     }
     seq_eam_force_tail(ctx, true, nullptr);
     if ((st = check_launch(ctx)) != MG_OK) return st;
@@ -1227,11 +1285,7 @@ static mg_status step_host_pipelined(mg_context *ctx, mg_atom_element *atoms, mg
     ctx->prepared = true;
     ctx->vmax_stale = true;
     ctx->energy_valid = false;
-    if (cnt[CNT_INTER] > 0) {
-        if ((st = mg_download(ctx, atoms, g.n_slots, inter, inter_cap, n_inter)) != MG_OK) return st;
-    } else {
-        *n_inter = 0;
-    }
+    *n_inter = cnt[CNT_INTER];  // 0: checked after decide
     return status_from_bits(ctx, static_cast<uint32_t>(cnt[CNT_ERRORS]));
 }
 

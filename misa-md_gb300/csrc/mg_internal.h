@@ -235,6 +235,11 @@ void launch_far_mark(const LaunchCtx &lc, const Geom &g, Inter in);
 void launch_ghost_copy(const LaunchCtx &lc, const Geom &g, Slots s, bool mixed);
 void launch_ghost_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool mixed);
 void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook);
+// the density pass over the sites [u0, u1) of both parities (as launch_lat_force_sites)
+void launch_lat_rho_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, int u0, int u1);
+// forward df for the ghost slots inside local planes [k0, k1), or (k0 < 0) the ghost planes below and
+// above the box plus the ghost inter atoms
+void launch_ghost_df_planes(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool mixed, int k0, int k1);
 void launch_lat_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook);
 void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *sp, bool kick,
                       bool mixed, bool hook);

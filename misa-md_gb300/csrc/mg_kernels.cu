@@ -622,6 +622,49 @@ void launch_ghost_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool
     if (mixed) k_ghost_df<true><<<n, b, 0, lc.stream>>>(g, s, in);
     else k_ghost_df<false><<<n, b, 0, lc.stream>>>(g, s, in);
 }
+// the same copy for the ghost slots inside the local planes [k0, k1) (y-ghost rows, then x-ghost
+// columns of each plane; their owners lie in the same plane), or (k0 < 0) for the ghost planes below
+// and above the box together with the ghost inter atoms
+template <bool MIXED>
+__global__ void k_ghost_df_planes(Geom g, Slots s, Inter in, int k0, int k1) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k0 < 0) {
+        if (t < 2 * g.gz * g.Sy * g.Sx) {
+            const int gs = ghost_slot(g, t);  // the z-ghost planes come first in the ghost enumeration
+            const int os = owner_slot(g, gs);
+            if (MIXED) s.df32[sidx(g, gs)] = s.df32[sidx(g, os)];
+            else s.df[gs] = s.df[os];
+        }
+        const int ng = in.cnt[CNT_GHOST];
+        for (int q = t; q < ng; q += gridDim.x * blockDim.x) in.gdf[q] = in.df[in.groot[q]];
+        return;
+    }
+    const int rows = 2 * g.gy * g.Sx, per = rows + 2 * g.gx * g.by;
+    if (t >= (k1 - k0) * per) return;
+    const int Z = g.gz + k0 + t / per, v = t % per;
+    int X, Y;
+    if (v < rows) {
+        const int yy = v / g.Sx;
+        Y = yy < g.gy ? yy : yy + g.by;
+        X = v % g.Sx;
+    } else {
+        const int w = v - rows, xx = w % (2 * g.gx);
+        X = xx < g.gx ? xx : xx + g.bx;
+        Y = g.gy + w / (2 * g.gx);
+    }
+    const int gs = lin(g, X, Y, Z);
+    const int os = owner_slot(g, gs);
+    if (MIXED) s.df32[sidx(g, gs)] = s.df32[sidx(g, os)];
+    else s.df[gs] = s.df[os];
+}
+void launch_ghost_df_planes(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool mixed, int k0, int k1) {
+    const int b = 256;
+    const int work = k0 < 0 ? 2 * g.gz * g.Sy * g.Sx : (k1 - k0) * (2 * g.gy * g.Sx + 2 * g.gx * g.by);
+    if (work <= 0) return;
+    const int n = (work + b - 1) / b;
+    if (mixed) k_ghost_df_planes<true><<<n, b, 0, lc.stream>>>(g, s, in, k0, k1);
+    else k_ghost_df_planes<false><<<n, b, 0, lc.stream>>>(g, s, in, k0, k1);
+}
 
 // ------------------------------------------------------------------------------------------------
 // lattice density pass (atom::latRho, src/atom.cpp:151-192, as a full gather) with dF/drho fused
@@ -689,8 +732,9 @@ __device__ __forceinline__ void k_lat_rho_fp64_site(int t, const NeighTables &nt
     }
 }
 template <bool LOOP>  // LOOP: several sites per thread, one grid stride apart
-__global__ void __launch_bounds__(512) k_lat_rho_fp64(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool hook, int order, int nthreads) {
-    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(512) k_lat_rho_fp64(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool hook, int order, int tbase,
+                                                       int nthreads) {
+    const int t0 = tbase + blockIdx.x * blockDim.x + threadIdx.x;  // threads [tbase, nthreads)
     if (!LOOP) {
         if (t0 < nthreads) k_lat_rho_fp64_site(t0, nt, g, s, in, pt, hook, order);
         return;
@@ -750,8 +794,9 @@ __device__ __forceinline__ void k_lat_rho_mixed_site(int t, const NeighTables &n
     }
 }
 template <bool LOOP>  // LOOP: several sites per thread, one grid stride apart
-__global__ void __launch_bounds__(512) k_lat_rho_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool hook, int order, int nthreads) {
-    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(512) k_lat_rho_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool hook, int order, int tbase,
+                                                       int nthreads) {
+    const int t0 = tbase + blockIdx.x * blockDim.x + threadIdx.x;  // threads [tbase, nthreads)
     if (!LOOP) {
         if (t0 < nthreads) k_lat_rho_mixed_site(t0, nt, g, s, in, pt, hook, order);
         return;
@@ -759,18 +804,41 @@ __global__ void __launch_bounds__(512) k_lat_rho_mixed(const __grid_constant__ N
     for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x) k_lat_rho_mixed_site(t, nt, g, s, in, pt, hook, order);
 }
 
-void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook) {
-    // atoms per thread: each thread takes rho_apt sites, one grid stride apart (the stride is a
-    // multiple of 64, so warps keep their parity and thread order)
-    const int order = lc.rho_order, b = lc.rho_block, nthr = gather_threads(g, order);
-    const int n = (nthr + b * lc.rho_apt - 1) / (b * lc.rho_apt);
+// atoms per thread: each thread takes rho_apt sites, one grid stride apart (the stride is a multiple
+// of 64, so warps keep their parity and thread order)
+static void launch_lat_rho_threads(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook,
+                                   int tb, int te) {
+    const int order = lc.rho_order, b = lc.rho_block;
+    const int n = (te - tb + b * lc.rho_apt - 1) / (b * lc.rho_apt);
+    if (n <= 0) return;
     if (lc.rho_apt > 1) {
-        if (mixed) k_lat_rho_mixed<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, nthr);
-        else k_lat_rho_fp64<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, nthr);
+        if (mixed) k_lat_rho_mixed<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, tb, te);
+        else k_lat_rho_fp64<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, tb, te);
     } else {
-        if (mixed) k_lat_rho_mixed<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, nthr);
-        else k_lat_rho_fp64<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, nthr);
+        if (mixed) k_lat_rho_mixed<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, tb, te);
+        else k_lat_rho_fp64<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, tb, te);
     }
+}
+void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook) {
+    launch_lat_rho_threads(lc, g, s, in, t, mixed, hook, 0, gather_threads(g, lc.rho_order));
+}
+// thread range of the sites [u0, u1) of both parities (u0, u1 multiples of 32, or u1 = n_local_half)
+static void site_threads(const Geom &g, int order, int u0, int u1, int tb[2], int te[2], int &nr) {
+    if (order) {  // warp w of parity p covers sites 32 (w / 2) .. + 31: thread t = 64 (u / 32) + 32 p + u % 32
+        tb[0] = (u0 >> 5) << 6;
+        te[0] = u1 >= g.n_local_half ? gather_threads(g, 1) : (u1 >> 5) << 6;
+        nr = 1;
+    } else {      // parity-major threads: one range per parity
+        tb[0] = u0; te[0] = u1;
+        tb[1] = g.n_local_half + u0; te[1] = g.n_local_half + u1;
+        nr = 2;
+    }
+}
+void launch_lat_rho_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, int u0, int u1) {
+    if (u1 <= u0) return;
+    int tb[2], te[2], nr;
+    site_threads(g, lc.rho_order, u0, u1, tb, te, nr);
+    for (int r = 0; r < nr; r++) launch_lat_rho_threads(lc, g, s, in, t, mixed, false, tb[r], te[r]);
 }
 
 // dF/drho when inter atoms added density after the lattice pass (or for the df hook)
@@ -998,14 +1066,9 @@ void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, Pot
 void launch_lat_force_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *p, bool kick,
                             bool mixed, int u0, int u1) {
     if (u1 <= u0) return;
-    if (lc.force_order) {  // warp w of parity p covers sites 32 (w / 2) .. + 31: thread t = 64 (u / 32) + 32 p + u % 32
-        const int tb = (u0 >> 5) << 6;
-        const int te = u1 >= g.n_local_half ? gather_threads(g, 1) : (u1 >> 5) << 6;
-        launch_lat_force_threads(lc, g, s, in, t, p, kick, mixed, false, tb, te);
-    } else {               // parity-major threads: one launch per parity
-        launch_lat_force_threads(lc, g, s, in, t, p, kick, mixed, false, u0, u1);
-        launch_lat_force_threads(lc, g, s, in, t, p, kick, mixed, false, g.n_local_half + u0, g.n_local_half + u1);
-    }
+    int tb[2], te[2], nr;
+    site_threads(g, lc.force_order, u0, u1, tb, te, nr);
+    for (int r = 0; r < nr; r++) launch_lat_force_threads(lc, g, s, in, t, p, kick, mixed, false, tb[r], te[r]);
 }
 
 // second half-kick for lattice slots (only when inter atoms prevented fusion, or always) and for
