@@ -539,10 +539,11 @@ def run_ours(args):
 
     if rank != 0:
         return
-    traffic = None
+    traffic, limiter = None, None
     try:
         tr = json.load(open(os.path.join(ROOT, "profiles", "lat_force_mixed_traffic.json")))
         traffic = tr["dram_bytes_per_launch"] / tr["atoms"] * n_atoms
+        limiter = tr.get("limiter")
     except (OSError, ValueError, KeyError):
         pass
     line = {
@@ -566,7 +567,8 @@ def run_ours(args):
                      "kernel": "lat_force (mixed)", "kernel_ms": force_ms,
                      "bytes_per_atom": BYTES_PER_ATOM_FORCE_SWEEP, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                      "traffic_source": "profiles/lat_force_mixed_traffic.json (ncu dram bytes, scaled by atoms)",
-                     "step_achieved_gbs": step_achieved, "step_frac": step_achieved / hbm_peak},
+                     "step_achieved_gbs": step_achieved, "step_frac": step_achieved / hbm_peak,
+                     "limiter": limiter},
         "kernel_ms_per_step": kt,
         "ms_per_step_instrumented": ms_instr / args.steps,
         "fp64": {"value": value64, "ms_per_step": ms64, "steps": args.fp64_steps},
