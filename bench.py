@@ -550,7 +550,8 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
-        "dtype_detail": "f32 distances, spline lookups and pair terms; Kahan-compensated f32 sums; f64 positions, "
+        "dtype_detail": "f32 distances, spline lookups and pair terms; Kahan-compensated f32 density sums, f32 "
+                        "force sums; f64 positions, "
                         "velocities, Verlet and reductions", "data": "synthetic",
         "config": {"workload": f"{w.name}: BCC Fe-1.5at%Cu-1.0at%Ni, {w.cells[0]}^3 unit cells = {n_atoms} atoms, "
                                f"{w.temperature:.0f} K Maxwell start, dt {w.dt * 1000:.0f} fs, synthetic 3-element setfl "

@@ -168,11 +168,6 @@ __device__ __forceinline__ f2 f2_pack(float lo, float hi) {
 __device__ __forceinline__ void f2_unpack(f2 a, float &lo, float &hi) {
     asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
 }
-__device__ __forceinline__ f2 f2_add(f2 a, f2 b) {
-    f2 r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
-    return r;
-}
 __device__ __forceinline__ f2 f2_sub(f2 a, f2 b) {
     f2 r;
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
@@ -187,13 +182,6 @@ __device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
     f2 r;
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
     return r;
-}
-// Kahan step on both lanes: sum += x with the compensation carried in comp
-__device__ __forceinline__ void kahan2(f2 &sum, f2 &comp, f2 x) {
-    const f2 y = f2_sub(x, comp);
-    const f2 t = f2_add(sum, y);
-    comp = f2_sub(f2_sub(t, sum), y);
-    sum = t;
 }
 __device__ __forceinline__ double dt_inv_m_of(const StepParams *p, int type) {
     return type == 0 ? p->dt_inv_m[0] : (type == 1 ? p->dt_inv_m[1] : p->dt_inv_m[2]);
@@ -954,7 +942,7 @@ __global__ void __launch_bounds__(512) k_lat_force_fp64(const __grid_constant__ 
 
 template <int PAR>
 __device__ __forceinline__ void force_sum_mixed(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int si, int ti,
-                                                float4 ui, float dfi, int q0, int q1, f2 &sxy, f2 &cxy, float &sz, float &cz) {
+                                                float4 ui, float dfi, int q0, int q1, f2 &sxy, float &sz) {
     // records of the pair row ti; the table constants are read from the parameter bank where used
     const int fbase = (ti * 3) * pt.nr;
     const f2 uixy = f2_pack(ui.x, ui.y);
@@ -990,8 +978,10 @@ __device__ __forceinline__ void force_sum_mixed(const NeighTables &nt, const Geo
             const float phip = (zp - phi) * rinv;
             const float psip = dfi * rhojp + __ldg(s.df32 + oj) * rhoip + phip;
             const float fpair = -psip * rinv;
-            kahan2(sxy, cxy, f2_mul(dxy, f2_pack(fpair, fpair)));
-            kahan(sz, cz, dz * fpair);
+            // plain FP32 accumulation: compensating it changed the force error by less than 1e-7 eV/A
+            // RMS and cost 7% of the pass
+            sxy = f2_fma(dxy, f2_pack(fpair, fpair), sxy);
+            sz = fmaf(dz, fpair, sz);
         }
     }
 }
@@ -1006,24 +996,23 @@ __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables 
     const int ti = __float_as_int(ui.w);
     if (ti < 0) { s.fx[sl] = 0.0; s.fy[sl] = 0.0; s.fz[sl] = 0.0; return; }
     const float dfi = s.df32[si];
-    // force sums (x and y packed, z) with their Kahan compensations
-    f2 sxy = f2_pack(0.f, 0.f), cxy = f2_pack(0.f, 0.f);
-    float sz = 0.f, cz = 0.f;
+    // force sums (x and y packed, z)
+    f2 sxy = f2_pack(0.f, 0.f);
+    float sz = 0.f;
     const int np = nt.npruned;
-    if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, 0, np, sxy, cxy, sz, cz);
-    else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, 0, np, sxy, cxy, sz, cz);
+    if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, 0, np, sxy, sz);
+    else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, 0, np, sxy, sz);
     if (in.far_flag[sl]) {
         const int nf = nt.nfull;
-        if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, np, nf, sxy, cxy, sz, cz);
-        else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, np, nf, sxy, cxy, sz, cz);
+        if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, np, nf, sxy, sz);
+        else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, np, nf, sxy, sz);
     }
-    float sx, sy, cx, cy;
+    float sx, sy;
     f2_unpack(sxy, sx, sy);
-    f2_unpack(cxy, cx, cy);
     const double h = 0.5 * g.a0;
-    const double fx = h * ((double) sx - (double) cx);
-    const double fy = h * ((double) sy - (double) cy);
-    const double fz = h * ((double) sz - (double) cz);
+    const double fx = h * (double) sx;
+    const double fy = h * (double) sy;
+    const double fz = h * (double) sz;
     s.fx[sl] = fx; s.fy[sl] = fy; s.fz[sl] = fz;
     if (kick && !hook && lattice_only(in)) {
         const double c = dt_inv_m_of(sp, ti);
