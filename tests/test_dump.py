@@ -216,3 +216,29 @@ def test_gpu_stage_machine_dumps(pkg, orc, wl, potentials, gpu_lib, tmp_path):
         assert np.abs(a["x"] - b["x"]).max() < 1e-9 and np.abs(a["v"] - b["v"]).max() < 1e-7
     ctx.set_stage_output()
     ctx.close()
+
+
+@pytest.mark.gpu
+def test_gpu_dump_reports_io_errors(pkg, wl, potentials, gpu_lib, tmp_path):
+    """An unwritable single-file path fails at open; an unwritable by-frame path fails in the writer
+    thread, and the failure comes back from the next frame or from close."""
+    cells = (8, 8, 8)
+    ctx = pkg.Context(cells, A0, RCF, precision="fp64")
+    ctx.pot_init_setfl(potentials["fe"])
+    ctx.upload(wl.build_state(cells, A0, RCF, temperature=300.0, seed=3))
+    missing = tmp_path / "no_such_dir"
+    with pytest.raises(pkg.MgError):
+        ctx.dump_open(str(missing / "d.out"))
+    d = ctx.dump_open(str(missing / "f_{}.out"), by_frame=True)
+    d.frame(1)
+    try:
+        d.frame(2)  # fails only if the writer has already met frame 1's error
+    except pkg.MgError:
+        pass
+    with pytest.raises(pkg.MgError, match="cannot write"):
+        d.close()
+    # the context stays usable
+    ok = ctx.dump_open(str(tmp_path / "ok.out"))
+    ok.frame(4)
+    assert ok.close() == 2 * 8 ** 3
+    ctx.close()
