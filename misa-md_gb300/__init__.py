@@ -124,6 +124,7 @@ _PROTOS = {
     "mg_dump_last_error": (ctypes.c_char_p, [_P]),
     "mg_set_stage_output": (_I32, [_P, _P, _U64, ctypes.c_char_p]),
     "mg_set_host_pipeline": (_I32, [_P, _I32]),
+    "mg_set_step_fusion": (_I32, [_P, _I32]),
 }
 
 
@@ -396,6 +397,10 @@ class Context:
 
     def eam_force_calc(self, atoms):
         self._check(self.lib.mg_eam_force_calc(self.h, _ptr(atoms), self.cutoff_radius))
+
+    def set_step_fusion(self, steps_per_graph):
+        """Loop bodies per graph launch of simulate in the mixed form (fused firststep; 0 or 1: off)."""
+        self._check(self.lib.mg_set_step_fusion(self.h, int(steps_per_graph)))
 
     def set_host_pipeline(self, chunks):
         """z-slabs of step_host's copy/compute pipeline (0 or 1: off)."""

@@ -69,6 +69,10 @@ struct mg_context {
     uint32_t *d_ws_flags = nullptr;
     int64_t ws_cap = 0;
     cudaGraphExec_t graph_exec = nullptr;
+    // fused multi-step graph: fuse_steps loop bodies whose force passes (all but the last) take the
+    // next firststep (mixed form, fixed dt); < 2: off
+    int fuse_steps = 16;
+    cudaGraphExec_t graph_multi = nullptr;
     bool graph_stale = true;
     uint64_t gen = 1;               // bumped whenever captured graphs of this context go stale
     int graph_prec = -1;
@@ -161,9 +165,9 @@ struct Timer {
 };
 
 // ---- the kernel sequences ----
-void seq_firststep(mg_context *ctx, bool decide, Timer *t) {
+void seq_firststep(mg_context *ctx, bool decide, Timer *t, bool fused = false) {
     const LaunchCtx lc = ctx->lc();
-    launch_firststep(lc, ctx->g, ctx->s, ctx->in, ctx->d_sp, decide);
+    launch_firststep(lc, ctx->g, ctx->s, ctx->in, ctx->d_sp, decide, 0, -1, fused);
     if (t) t->mark(1);
     launch_inter_firststep(lc, ctx->in, ctx->d_sp);
     if (t) t->mark(2);
@@ -205,20 +209,24 @@ void seq_eam_force_tail(mg_context *ctx, bool kick, Timer *t) {
     if (kick) launch_secondstep(lc, ctx->g, ctx->s, ctx->in, ctx->d_sp, false);
     if (t) t->mark(11);
 }
-void seq_compute_eam(mg_context *ctx, bool kick, bool with_manage_prefix, int manage_mask, Timer *t) {
+void seq_compute_eam(mg_context *ctx, bool kick, bool with_manage_prefix, int manage_mask, Timer *t, bool fuse_next = false) {
     seq_eam_lists(ctx, with_manage_prefix, manage_mask, t);
     seq_eam_rho(ctx, t);
-    launch_lat_force(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, kick, ctx->mixed(), false);
+    launch_lat_force(ctx->lc(), ctx->g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, kick, ctx->mixed(), false, fuse_next);
     if (t) t->mark(9);
     seq_eam_force_tail(ctx, kick, t);
 }
-// one loop body: firststep, decide, exchangeInter, borderInter, exchangeAtom, computeEam, secondstep
-void seq_step(mg_context *ctx, Timer *t) {
+// one loop body: firststep, decide, exchangeInter, borderInter, exchangeAtom, computeEam, secondstep.
+// fused_prev: the previous body's force pass took this firststep; fuse_next: this force pass takes the
+// next one (both only act when no inter atoms exist, which the kernels check on the device)
+void seq_step(mg_context *ctx, Timer *t, bool fused_prev = false, bool fuse_next = false) {
     if (t) t->mark(0);
     launch_step_head(ctx->lc(), ctx->d_sp);
-    seq_firststep(ctx, true, t);
-    seq_compute_eam(ctx, true, true, MANAGE_DECIDE | MANAGE_CLEAR_GHOST | MANAGE_EXCHANGE | MANAGE_BORDER, t);
+    seq_firststep(ctx, true, t, fused_prev);
+    seq_compute_eam(ctx, true, true, MANAGE_DECIDE | MANAGE_CLEAR_GHOST | MANAGE_EXCHANGE | MANAGE_BORDER, t, fuse_next);
 }
+// steps of mg_simulate that run fused: the mixed form with a fixed dt
+bool fusable(const mg_context *ctx) { return ctx->fuse_steps >= 2 && ctx->mixed() && ctx->dx_max <= 0.0; }
 constexpr int kLaunchesPerStep = 17;
 
 mg_status require_ready(mg_context *ctx) {
@@ -367,6 +375,7 @@ mg_status check_types(mg_context *ctx, const mg_atom_element *atoms, int64_t n) 
 mg_status build_graph(mg_context *ctx) {
     if (ctx->graph_exec && !ctx->graph_stale && ctx->graph_prec == ctx->precision) return MG_OK;
     if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
+    if (ctx->graph_multi) { cudaGraphExecDestroy(ctx->graph_multi); ctx->graph_multi = nullptr; }
     cudaGraph_t graph;
     MG_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     seq_step(ctx, nullptr);
@@ -379,6 +388,22 @@ mg_status build_graph(mg_context *ctx) {
     if (e != cudaSuccess) { ctx->err = std::string("graph instantiate: ") + cudaGetErrorString(e); return MG_ERR_CUDA; }
     ctx->graph_stale = false;
     ctx->graph_prec = ctx->precision;
+    return MG_OK;
+}
+
+// fuse_steps loop bodies in one graph: the first takes its own firststep, the last does not take the
+// next one, so the state between launches is the end of a loop body as always
+mg_status build_graph_multi(mg_context *ctx) {
+    mg_status st = build_graph(ctx);
+    if (st != MG_OK || ctx->graph_multi) return st;
+    cudaGraph_t graph;
+    MG_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const int k = ctx->fuse_steps;
+    for (int i = 0; i < k; i++) seq_step(ctx, nullptr, i > 0, i < k - 1);
+    MG_CK(cudaStreamEndCapture(ctx->stream, &graph));
+    cudaError_t e = cudaGraphInstantiate(&ctx->graph_multi, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { ctx->err = std::string("graph instantiate: ") + cudaGetErrorString(e); return MG_ERR_CUDA; }
     return MG_OK;
 }
 
@@ -492,7 +517,7 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     ALLOC(s.fx, ns); ALLOC(s.fy, ns); ALLOC(s.fz, ns);
     ALLOC(s.rho, ns); ALLOC(s.df, ns); ALLOC(s.e, ns);
     ALLOC(s.type, ns); ALLOC(s.id, ns);
-    ALLOC(s.u4, ns); ALLOC(s.df32, ns);
+    ALLOC(s.u4, ns); ALLOC(s.u4n, ns); ALLOC(s.df32, ns);
 
     Inter &in = ctx->in;
     in.cap = static_cast<int>(inter_capacity > 0 ? inter_capacity : 16384);
@@ -541,6 +566,7 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
                             ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s.type, 0xff, ns, ctx->stream);  // all slots INVALID
     if (e == cudaSuccess) e = cudaMemsetAsync(s.u4, 0xff, ns * sizeof(float4), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s.u4n, 0xff, ns * sizeof(float4), ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_sp, 0, sizeof(StepParams), ctx->stream);
     if (e != cudaSuccess) return fail(e);
     if (upload_tables(ctx) != MG_OK) { g_create_error = ctx->err; mg_destroy(ctx); return MG_ERR_CUDA; }
@@ -554,6 +580,7 @@ mg_status mg_destroy(mg_context *ctx) {
     if (!ctx) return MG_ERR_ARG;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->graph_multi) cudaGraphExecDestroy(ctx->graph_multi);
     for (cudaEvent_t e : ctx->ev) cudaEventDestroy(e);
     for (cudaEvent_t e : ctx->pipe_ev) cudaEventDestroy(e);
     if (ctx->copy_in) cudaStreamDestroy(ctx->copy_in);
@@ -865,9 +892,14 @@ mg_status mg_simulate(mg_context *ctx, int64_t nsteps, int32_t sync) {
             MG_CK(cudaEventCreate(&e));
             ctx->ev.push_back(e);
         }
+        // the same fusion pattern as the graphs: blocks of fuse_steps bodies, then single bodies
+        const bool fuse = fusable(ctx) && nsteps >= 2;
+        const int64_t k = fuse ? ctx->fuse_steps : 1, blocks = fuse ? nsteps / k : 0;
         for (int64_t i = 0; i < nsteps; i++) {
             Timer t{ctx, i};
-            seq_step(ctx, &t);
+            const bool in_block = i < blocks * k;
+            const int64_t pos = i % k;
+            seq_step(ctx, &t, in_block && pos > 0, in_block && pos < k - 1);
         }
         if ((st = check_launch(ctx)) != MG_OK) return st;
         MG_CK(cudaStreamSynchronize(ctx->stream));
@@ -882,7 +914,12 @@ mg_status mg_simulate(mg_context *ctx, int64_t nsteps, int32_t sync) {
         ctx->timed_steps = nsteps;
     } else {
         if ((st = build_graph(ctx)) != MG_OK) return st;
-        for (int64_t i = 0; i < nsteps; i++) MG_CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+        int64_t i = 0;
+        if (fusable(ctx) && nsteps >= ctx->fuse_steps) {
+            if ((st = build_graph_multi(ctx)) != MG_OK) return st;
+            for (; i + ctx->fuse_steps <= nsteps; i += ctx->fuse_steps) MG_CK(cudaGraphLaunch(ctx->graph_multi, ctx->stream));
+        }
+        for (; i < nsteps; i++) MG_CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
     }
     ctx->energy_valid = false;
     if (sync) {
@@ -1287,6 +1324,13 @@ static mg_status step_host_pipelined(mg_context *ctx, mg_atom_element *atoms, mg
     ctx->energy_valid = false;
     *n_inter = cnt[CNT_INTER];  // 0: checked after decide
     return status_from_bits(ctx, static_cast<uint32_t>(cnt[CNT_ERRORS]));
+}
+
+mg_status mg_set_step_fusion(mg_context *ctx, int32_t steps_per_graph) {
+    if (!ctx || steps_per_graph < 0 || steps_per_graph > 256) return MG_ERR_ARG;
+    ctx->fuse_steps = steps_per_graph;
+    if (ctx->graph_multi) { cudaGraphExecDestroy(ctx->graph_multi); ctx->graph_multi = nullptr; }
+    return MG_OK;
 }
 
 mg_status mg_set_host_pipeline(mg_context *ctx, int32_t chunks) {

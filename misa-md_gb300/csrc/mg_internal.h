@@ -82,6 +82,7 @@ struct Slots {
     uint64_t *id;
     // mixed form, parity-split layout (slot s at (s & 1) * half + (s >> 1)):
     float4 *u4;              // displacement from the site in half-lattice units, w = type bits
+    float4 *u4n;             // the next step's u4 when the force pass takes the next firststep
     float *df32;             // F'(rho) in float
 };
 
@@ -222,8 +223,9 @@ void launch_pack_aos(const LaunchCtx &lc, const Geom &g, mg_atom_element *aos, S
 enum { PACK_ALL = 0xff, PACK_RHO = 1, PACK_DF = 2, PACK_F = 4 };
 
 // local atoms [t0, t1) in k, j, i order (t1 < 0: all)
+// fused: the previous force pass took this firststep already (launch_lat_force with fuse_next)
 void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const StepParams *sp, bool decide, int t0 = 0,
-                      int t1 = -1);
+                      int t1 = -1, bool fused = false);
 // fill g.site_half (once per context)
 void launch_site_table(const LaunchCtx &lc, const Geom &g, double *site_half);
 void launch_decide_scan(const LaunchCtx &lc, const Geom &g, Slots s, Inter in);
@@ -241,8 +243,10 @@ void launch_lat_rho_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in,
 // above the box plus the ghost inter atoms
 void launch_ghost_df_planes(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool mixed, int k0, int k1);
 void launch_lat_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook);
+// fuse_next (mixed form, kick, fixed dt): after the second half-kick each lattice atom also takes the
+// next step's firststep (into u4n), when no inter atoms exist
 void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *sp, bool kick,
-                      bool mixed, bool hook);
+                      bool mixed, bool hook, bool fuse_next = false);
 // the force pass over the sites of both parities whose index within their parity is in [u0, u1):
 // with u0 and u1 multiples of 32 (or u1 = n_local_half) the slabs of a split pass are disjoint warps
 void launch_lat_force_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *sp, bool kick,

@@ -370,25 +370,20 @@ __device__ __noinline__ bool exact_displaced(double ex, double ey, double ez, do
     return d;
 }
 
+// NewtonMotion::firststep for one lattice atom (src/newton_motion.cpp:30-55) and decide's displacement
+// test (src/atom.cpp:34-42): v += c f, x += dt v (each operation rounded as the reference rounds it),
+// the displacement record u4 (written to u4_out, parity-split index) and the displaced flag of local
+// index t. MOVE = false: the test alone, on the current positions.
 template <bool MOVE, bool DECIDE>
-__global__ void __launch_bounds__(kFirstThreads) k_firststep(Geom g, Slots s, Inter in, const StepParams *__restrict__ p,
-                                                             int t0, int t1) {
-    const int t = t0 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= t1) return;
-    int i, j, k;
-    const int sl = local_slot(g, t, i, j, k);
-    const int ty = s.type[sl];
-    if (ty < 0) {
-        if (DECIDE) in.dflag[t] = 0;
-        return;
-    }
+__device__ __forceinline__ void first_half(const Geom &g, const Slots &s, const Inter &in, const StepParams *__restrict__ p,
+                                           int sl, int t, int i, int j, int k, int ty, double vx, double vy, double vz,
+                                           double fx, double fy, double fz, float4 *u4_out) {
     double x = s.x[sl], y = s.y[sl], z = s.z[sl];
     if (MOVE) {
         const double c = dt_inv_m_of(p, ty);
-        double vx = s.vx[sl], vy = s.vy[sl], vz = s.vz[sl];
-        vx = __dadd_rn(vx, __dmul_rn(c, s.fx[sl]));
-        vy = __dadd_rn(vy, __dmul_rn(c, s.fy[sl]));
-        vz = __dadd_rn(vz, __dmul_rn(c, s.fz[sl]));
+        vx = __dadd_rn(vx, __dmul_rn(c, fx));
+        vy = __dadd_rn(vy, __dmul_rn(c, fy));
+        vz = __dadd_rn(vz, __dmul_rn(c, fz));
         const double dt = p->dt;
         x = __dadd_rn(x, __dmul_rn(dt, vx));
         y = __dadd_rn(y, __dmul_rn(dt, vy));
@@ -404,7 +399,7 @@ __global__ void __launch_bounds__(kFirstThreads) k_firststep(Geom g, Slots s, In
     const float exf = __double2float_rn(ex), eyf = __double2float_rn(ey), ezf = __double2float_rn(ez);
     if (MOVE) {
         const float ih = g.inv_h_f;
-        s.u4[sidx(g, sl)] = make_float4(exf * ih, eyf * ih, ezf * ih, __int_as_float(ty));
+        u4_out[sidx(g, sl)] = make_float4(exf * ih, eyf * ih, ezf * ih, __int_as_float(ty));
     }
     if (DECIDE) {
         // the exact FP64 test of decide runs only where the FP32 distance is not clearly below it
@@ -413,6 +408,31 @@ __global__ void __launch_bounds__(kFirstThreads) k_firststep(Geom g, Slots s, In
                           exact_displaced(ex, ey, ez, g.thr, &in.cnt[CNT_DISP_RAW]);
         in.dflag[t] = disp ? 1 : 0;
     }
+}
+
+// fused: the previous step's force pass already took this firststep for every lattice atom (when no
+// inter atoms exist); only the displacement records it left in u4n move into u4
+template <bool MOVE, bool DECIDE>
+__global__ void __launch_bounds__(kFirstThreads) k_firststep(Geom g, Slots s, Inter in, const StepParams *__restrict__ p,
+                                                             int t0, int t1, bool fused) {
+    const int t = t0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= t1) return;
+    int i, j, k;
+    const int sl = local_slot(g, t, i, j, k);
+    const int ty = s.type[sl];
+    if (fused && lattice_only(in)) {
+        if (ty >= 0) s.u4[sidx(g, sl)] = s.u4n[sidx(g, sl)];
+        return;
+    }
+    if (ty < 0) {
+        if (DECIDE) in.dflag[t] = 0;
+        return;
+    }
+    if (MOVE)
+        first_half<true, DECIDE>(g, s, in, p, sl, t, i, j, k, ty, s.vx[sl], s.vy[sl], s.vz[sl], s.fx[sl], s.fy[sl],
+                                 s.fz[sl], s.u4);
+    else
+        first_half<false, DECIDE>(g, s, in, p, sl, t, i, j, k, ty, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, s.u4);
 }
 
 // one warp per group of kFirstThreads flag bytes (8 per lane, read as one 64-bit word): its count
@@ -501,16 +521,16 @@ __global__ void k_disp_collect(Geom g, Inter in, int nblocks) {
 }
 
 void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const StepParams *p, bool decide, int t0,
-                      int t1) {
+                      int t1, bool fused) {
     if (t1 < 0) t1 = g.n_local;
     if (t1 <= t0) return;
     const int b = kFirstThreads, n = (t1 - t0 + b - 1) / b;
-    if (decide) k_firststep<true, true><<<n, b, 0, lc.stream>>>(g, s, in, p, t0, t1);
-    else k_firststep<true, false><<<n, b, 0, lc.stream>>>(g, s, in, p, t0, t1);
+    if (decide) k_firststep<true, true><<<n, b, 0, lc.stream>>>(g, s, in, p, t0, t1, fused);
+    else k_firststep<true, false><<<n, b, 0, lc.stream>>>(g, s, in, p, t0, t1, fused);
 }
 void launch_decide_scan(const LaunchCtx &lc, const Geom &g, Slots s, Inter in) {
     const int b = kFirstThreads, n = (g.n_local + b - 1) / b;
-    k_firststep<false, true><<<n, b, 0, lc.stream>>>(g, s, in, nullptr, 0, g.n_local);
+    k_firststep<false, true><<<n, b, 0, lc.stream>>>(g, s, in, nullptr, 0, g.n_local, false);
 }
 void launch_displaced_collect(const LaunchCtx &lc, const Geom &g, Inter in) {
     const int nblocks = (g.n_local + kFirstThreads - 1) / kFirstThreads;
@@ -986,15 +1006,32 @@ __device__ __forceinline__ void force_sum_mixed(const NeighTables &nt, const Geo
     }
 }
 
+// local coordinates and local index (k, j, i order) of a local slot
+__device__ __forceinline__ int local_index_of(const Geom &g, int sl, int &i, int &j, int &k) {
+    const int X = sl % g.Sx, r = sl / g.Sx;
+    i = X - g.gx;
+    j = r % g.Sy - g.gy;
+    k = r / g.Sy - g.gz;
+    return (k * g.by + j) * g.bx + i;
+}
+
 __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables &nt, const Geom &g, const Slots &s, const Inter &in,
-                                                const PotTables &pt, StepParams *sp, bool kick, bool hook, int order) {
+                                                const PotTables &pt, StepParams *sp, bool kick, bool hook, int order,
+                                                bool fuse_next) {
     int par;
     const int sl = gather_slot(g, t, order, par);
     if (sl < 0) return;
     const int si = sidx(g, sl);
     const float4 ui = s.u4[si];
     const int ti = __float_as_int(ui.w);
-    if (ti < 0) { s.fx[sl] = 0.0; s.fy[sl] = 0.0; s.fz[sl] = 0.0; return; }
+    if (ti < 0) {
+        s.fx[sl] = 0.0; s.fy[sl] = 0.0; s.fz[sl] = 0.0;
+        if (fuse_next && lattice_only(in)) {  // the next firststep's flag of a vacancy
+            int i, j, k;
+            in.dflag[local_index_of(g, sl, i, j, k)] = 0;
+        }
+        return;
+    }
     const float dfi = s.df32[si];
     // force sums (x and y packed, z)
     f2 sxy = f2_pack(0.f, 0.f);
@@ -1019,38 +1056,47 @@ __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables 
         const double vx = __dadd_rn(s.vx[sl], __dmul_rn(c, fx));
         const double vy = __dadd_rn(s.vy[sl], __dmul_rn(c, fy));
         const double vz = __dadd_rn(s.vz[sl], __dmul_rn(c, fz));
-        s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz;
+        if (!fuse_next) { s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz; }  // else first_half writes the next v
         note_vmax2(sp, speed2(vx, vy, vz));
+        if (fuse_next) {
+            // the next loop body's firststep for this atom, with the force still in registers (the
+            // other threads of this pass still read this atom's u4, so the new record goes to u4n)
+            int i, j, k;
+            const int tl = local_index_of(g, sl, i, j, k);
+            first_half<true, true>(g, s, in, sp, sl, tl, i, j, k, ti, vx, vy, vz, fx, fy, fz, s.u4n);
+        }
     }
 }
 template <bool LOOP>  // LOOP: several sites per thread, one grid stride apart
 __global__ void __launch_bounds__(512, 3) k_lat_force_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt,
                                                          StepParams *sp, bool kick, bool hook, int order, int tbase,
-                                                         int nthreads) {
+                                                         int nthreads, bool fuse_next) {
     const int t0 = tbase + blockIdx.x * blockDim.x + threadIdx.x;  // threads [tbase, nthreads)
     if (!LOOP) {
-        if (t0 < nthreads) k_lat_force_mixed_site(t0, nt, g, s, in, pt, sp, kick, hook, order);
+        if (t0 < nthreads) k_lat_force_mixed_site(t0, nt, g, s, in, pt, sp, kick, hook, order, fuse_next);
         return;
     }
-    for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x) k_lat_force_mixed_site(t, nt, g, s, in, pt, sp, kick, hook, order);
+    for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x)
+        k_lat_force_mixed_site(t, nt, g, s, in, pt, sp, kick, hook, order, fuse_next);
 }
 
 static void launch_lat_force_threads(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *p,
-                                     bool kick, bool mixed, bool hook, int tb, int te) {
+                                     bool kick, bool mixed, bool hook, int tb, int te, bool fuse_next = false) {
     const int order = lc.force_order, b = lc.force_block;
     const int n = (te - tb + b * lc.force_apt - 1) / (b * lc.force_apt);
     if (n <= 0) return;
+    const bool fuse = fuse_next && mixed && kick && !hook;
     if (lc.force_apt > 1) {
-        if (mixed) k_lat_force_mixed<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te);
+        if (mixed) k_lat_force_mixed<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te, fuse);
         else k_lat_force_fp64<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te);
     } else {
-        if (mixed) k_lat_force_mixed<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te);
+        if (mixed) k_lat_force_mixed<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te, fuse);
         else k_lat_force_fp64<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te);
     }
 }
 void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *p, bool kick,
-                      bool mixed, bool hook) {
-    launch_lat_force_threads(lc, g, s, in, t, p, kick, mixed, hook, 0, gather_threads(g, lc.force_order));
+                      bool mixed, bool hook, bool fuse_next) {
+    launch_lat_force_threads(lc, g, s, in, t, p, kick, mixed, hook, 0, gather_threads(g, lc.force_order), fuse_next);
 }
 void launch_lat_force_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *p, bool kick,
                             bool mixed, int u0, int u1) {

@@ -100,3 +100,39 @@ def test_pipelined_step_host_matches_oracle(pkg, orc, wl, potentials, gpu_lib):
     assert np.abs(got["x"][loc] - w["x"][loc]).max() < 1e-12
     assert np.abs(got["f"][loc] - w["f"][loc]).max() < 1e-9
     cp.close()
+
+
+@pytest.mark.parametrize("timing", [False, True])
+def test_fused_firststep_is_bit_identical(pkg, wl, potentials, gpu_lib, timing):
+    """mg_simulate with the next firststep fused into the force pass (blocks of 4 bodies, then single
+    bodies) against one body per launch, bit for bit: first a thermal alloy (fusion active), then the
+    same state with a few atoms pushed off their sites, so inter atoms appear and the kernels fall
+    back to the separate firststep on the device."""
+    cells = (10, 9, 11)
+    atoms = wl.build_state(cells, A0, RCF, temperature=600.0, seed=31, cu_frac=0.05, ni_frac=0.03)
+    loc = wl.local_slot_indices(cells, RCF)
+    out = []
+    for fuse in (4, 0):
+        c = pkg.Context(cells, A0, RCF, precision="mixed", inter_capacity=256)
+        c.pot_init_setfl(potentials["fecuni"])
+        c.set_timestep(0.001)
+        c.set_step_fusion(fuse)
+        c.upload(atoms)
+        c.prepare()
+        c.enable_timing(timing)
+        c.simulate(11, sync=True)    # two fused blocks of 4, then 3 single bodies
+        mid, _ = c.download()
+        assert c.thermo()["n_inter"] == 0
+        pushed = mid.copy()
+        for k in (17, 400, 901):  # to an octahedral interstice: inter atoms for the rest of the run
+            pushed["x"][loc[k]] += A0 * np.array([0.5, 0.5, 0.0])
+        c.upload(pushed)
+        c.prepare()
+        c.simulate(9, sync=True)
+        a, inter = c.download()
+        out.append((mid, a, inter, c.thermo()["n_inter"]))
+        c.close()
+    (m1, a1, i1, n1), (m0, a0_, i0, n0) = out
+    assert m1.tobytes() == m0.tobytes()
+    assert n1 == n0 and n1 > 0
+    assert a1.tobytes() == a0_.tobytes() and i1.tobytes() == i0.tobytes()
