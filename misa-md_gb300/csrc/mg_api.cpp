@@ -73,6 +73,7 @@ struct mg_context {
     // next firststep (mixed form, fixed dt); < 2: off
     int fuse_steps = 16;
     cudaGraphExec_t graph_multi = nullptr;
+    float4 *u4_main = nullptr, *u4_alt = nullptr;  // s.u4 and s.u4n outside fused graphs
     bool graph_stale = true;
     uint64_t gen = 1;               // bumped whenever captured graphs of this context go stale
     int graph_prec = -1;
@@ -391,6 +392,14 @@ mg_status build_graph(mg_context *ctx) {
     return MG_OK;
 }
 
+// The u4 buffers of body i of k fused bodies: its own and the next body's alternate, and the last
+// body's own is the context's usual one, so between launches u4 is where every other call expects it.
+void set_body_buffers(mg_context *ctx, int64_t k, int64_t i) {
+    const bool own_is_main = ((k - 1 - i) % 2) == 0;
+    ctx->s.u4 = own_is_main ? ctx->u4_main : ctx->u4_alt;
+    ctx->s.u4n = own_is_main ? ctx->u4_alt : ctx->u4_main;
+}
+
 // fuse_steps loop bodies in one graph: the first takes its own firststep, the last does not take the
 // next one, so the state between launches is the end of a loop body as always
 mg_status build_graph_multi(mg_context *ctx) {
@@ -399,7 +408,11 @@ mg_status build_graph_multi(mg_context *ctx) {
     cudaGraph_t graph;
     MG_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     const int k = ctx->fuse_steps;
-    for (int i = 0; i < k; i++) seq_step(ctx, nullptr, i > 0, i < k - 1);
+    for (int i = 0; i < k; i++) {
+        set_body_buffers(ctx, k, i);
+        seq_step(ctx, nullptr, i > 0, i < k - 1);
+    }
+    set_body_buffers(ctx, k, k - 1);
     MG_CK(cudaStreamEndCapture(ctx->stream, &graph));
     cudaError_t e = cudaGraphInstantiate(&ctx->graph_multi, graph, 0);
     cudaGraphDestroy(graph);
@@ -518,6 +531,8 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     ALLOC(s.rho, ns); ALLOC(s.df, ns); ALLOC(s.e, ns);
     ALLOC(s.type, ns); ALLOC(s.id, ns);
     ALLOC(s.u4, ns); ALLOC(s.u4n, ns); ALLOC(s.df32, ns);
+    ctx->u4_main = s.u4;
+    ctx->u4_alt = s.u4n;
 
     Inter &in = ctx->in;
     in.cap = static_cast<int>(inter_capacity > 0 ? inter_capacity : 16384);
@@ -899,8 +914,10 @@ mg_status mg_simulate(mg_context *ctx, int64_t nsteps, int32_t sync) {
             Timer t{ctx, i};
             const bool in_block = i < blocks * k;
             const int64_t pos = i % k;
+            if (in_block) set_body_buffers(ctx, k, pos);
             seq_step(ctx, &t, in_block && pos > 0, in_block && pos < k - 1);
         }
+        set_body_buffers(ctx, 1, 0);
         if ((st = check_launch(ctx)) != MG_OK) return st;
         MG_CK(cudaStreamSynchronize(ctx->stream));
         ctx->timer_ms.assign(kNumTimers, 0.0);

@@ -82,7 +82,7 @@ struct Slots {
     uint64_t *id;
     // mixed form, parity-split layout (slot s at (s & 1) * half + (s >> 1)):
     float4 *u4;              // displacement from the site in half-lattice units, w = type bits
-    float4 *u4n;             // the next step's u4 when the force pass takes the next firststep
+    float4 *u4n;             // the next loop body's u4 buffer when the force pass takes the next firststep
     float *df32;             // F'(rho) in float
 };
 

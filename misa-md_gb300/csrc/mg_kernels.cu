@@ -410,22 +410,22 @@ __device__ __forceinline__ void first_half(const Geom &g, const Slots &s, const 
     }
 }
 
-// fused: the previous step's force pass already took this firststep for every lattice atom (when no
-// inter atoms exist); only the displacement records it left in u4n move into u4
+// fused: the previous step's force pass already took this firststep for every local slot and wrote
+// its displacement records into this step's u4 buffer (when no inter atoms exist; else the work is
+// done here). Every local slot's u4 is written, vacancies included, so the two buffers a fused graph
+// alternates between are always complete.
 template <bool MOVE, bool DECIDE>
 __global__ void __launch_bounds__(kFirstThreads) k_firststep(Geom g, Slots s, Inter in, const StepParams *__restrict__ p,
                                                              int t0, int t1, bool fused) {
     const int t = t0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= t1) return;
+    if (fused && lattice_only(in)) return;
     int i, j, k;
     const int sl = local_slot(g, t, i, j, k);
     const int ty = s.type[sl];
-    if (fused && lattice_only(in)) {
-        if (ty >= 0) s.u4[sidx(g, sl)] = s.u4n[sidx(g, sl)];
-        return;
-    }
     if (ty < 0) {
         if (DECIDE) in.dflag[t] = 0;
+        if (MOVE) s.u4[sidx(g, sl)] = vacant_u4();
         return;
     }
     if (MOVE)
@@ -1026,9 +1026,10 @@ __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables 
     const int ti = __float_as_int(ui.w);
     if (ti < 0) {
         s.fx[sl] = 0.0; s.fy[sl] = 0.0; s.fz[sl] = 0.0;
-        if (fuse_next && lattice_only(in)) {  // the next firststep's flag of a vacancy
+        if (fuse_next && lattice_only(in)) {  // the next firststep's flag and record of a vacancy
             int i, j, k;
             in.dflag[local_index_of(g, sl, i, j, k)] = 0;
+            s.u4n[si] = vacant_u4();
         }
         return;
     }
@@ -1060,7 +1061,8 @@ __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables 
         note_vmax2(sp, speed2(vx, vy, vz));
         if (fuse_next) {
             // the next loop body's firststep for this atom, with the force still in registers (the
-            // other threads of this pass still read this atom's u4, so the new record goes to u4n)
+            // other threads of this pass still read this atom's u4, so the new record goes to the next
+            // body's buffer, u4n)
             int i, j, k;
             const int tl = local_index_of(g, sl, i, j, k);
             first_half<true, true>(g, s, in, sp, sl, tl, i, j, k, ti, vx, vy, vz, fx, fy, fz, s.u4n);
