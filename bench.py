@@ -557,7 +557,8 @@ def run_ours(args):
                                f"{w.temperature:.0f} K Maxwell start, dt {w.dt * 1000:.0f} fs, synthetic 3-element setfl "
                                f"(nr = nrho = 5000, rc 5.6 A)",
                    "precision": "mixed", "l2": "working set ~1.9 GB > 129 MB L2 (no flush needed)",
-                   "timing": "value: CUDA-graph replay timed with CUDA events on the library stream; kernel times: "
+                   "timing": "value: CUDA-graph replay (16 loop bodies per launch, each force pass but the last taking "
+                             "the next body's firststep) timed with CUDA events on the library stream; kernel times: "
                              "a second pass of the same steps with events around every kernel",
                    "parallelism": f"{world} independent replica(s), one per GPU"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io,
