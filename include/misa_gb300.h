@@ -195,7 +195,8 @@ mg_status mg_step_host(mg_context *ctx, mg_atom_element *atoms, int64_t n_slots,
  * 1: one body per launch). Inside a launch, each force pass but the last also takes the next body's
  * firststep for its atoms (when no inter atoms exist; the kernels check on the device), which saves
  * the separate firststep pass. The state between launches is the end of a loop body as always, and
- * results are bit-identical either way. */
+ * results are bit-identical either way. mg_run_stages uses the same graph for runs of bodies with
+ * no stage event between them. */
 mg_status mg_set_step_fusion(mg_context *ctx, int32_t steps_per_graph);
 /* Number of z-slabs of mg_step_host's pipeline (default 16; 0 or 1: no pipelining). */
 mg_status mg_set_host_pipeline(mg_context *ctx, int32_t chunks);

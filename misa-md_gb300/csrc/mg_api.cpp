@@ -1112,7 +1112,28 @@ mg_status mg_run_stages(mg_context *ctx, const mg_stage *stages, int32_t n_stage
             launch_vmax_full(lc, ctx->g, ctx->s, ctx->in, ctx->d_sp);
             ctx->vmax_stale = false;
         }
-        MG_CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+        // a fused graph of fuse_steps bodies when none of them has an event inside the run: no stage
+        // change, PKA or rescale before bodies 1 .. k-1, no dump or thermo sample after bodies 0 .. k-2
+        const int64_t k = ctx->fuse_steps;
+        bool fused = fusable(ctx) && step + k <= steps;
+        for (int64_t j = 1; fused && j < k; j++) {
+            const int64_t css = cur_stage_steps + j, sj = step + j;
+            if (css >= stage_len || (cur->collision_set && css + 1 == cur->collision_step) ||
+                (cur->rescales_set && css % cur->rescale_every == 0))
+                fused = false;
+            const int64_t before = sj;  // body j - 1 ends at step number sj (1-based)
+            if ((ctx->stage_dump && ctx->stage_dump_interval && before % ctx->stage_dump_interval == 0) ||
+                (thermo_interval && before % thermo_interval == 0))
+                fused = false;
+        }
+        if (fused) {
+            if ((st = build_graph_multi(ctx)) != MG_OK) return st;
+            MG_CK(cudaGraphLaunch(ctx->graph_multi, ctx->stream));
+            cur_stage_steps += k - 1;
+            step += k - 1;
+        } else {
+            MG_CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+        }
         cur_stage_steps++;
         if (ctx->stage_dump && ctx->stage_dump_interval && (step + 1) % ctx->stage_dump_interval == 0) {
             if ((st = mg_dump_frame(ctx->stage_dump, static_cast<uint64_t>(step + 1))) != MG_OK) {

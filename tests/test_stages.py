@@ -67,3 +67,29 @@ def test_stage_machine_matches_the_reference_driver(pkg, orc, wl, potentials, gp
         ctx.run_stages([{"steps": 2}], 5, default_dt=0.001, n_atoms=n)   # runs out of stages
     assert e.value.status == 6
     ctx.close()
+
+
+def test_stage_machine_fused_bodies_are_bit_identical(pkg, wl, potentials, gpu_lib):
+    """Mixed form: runs of 16 event-free bodies go through the fused graph (firststep inside the force
+    pass); the samples and the final state equal those of one body per launch, bit for bit."""
+    cells = (10, 9, 9)
+    n = 2 * 10 * 9 * 9
+    atoms = wl.build_state(cells, A0, RCF, temperature=300.0, seed=5)
+    stages = [
+        {"steps": 70, "step_length": 0.0005, "rescale_t": 600.0, "rescale_every": 35},
+        {"steps": 60, "collision_step": 27, "lat": [4, 4, 4, 1], "direction": [1.0, 2.0, 2.5], "energy": 150.0},
+    ]
+    out = []
+    for fuse in (16, 0):
+        ctx = pkg.Context(cells, A0, RCF, precision="mixed", inter_capacity=1024)
+        ctx.pot_init_setfl(potentials["fe"])
+        ctx.set_step_fusion(fuse)
+        ctx.upload(atoms)
+        ctx.prepare()
+        got = ctx.run_stages(stages, 130, default_dt=0.001, n_atoms=n, thermo_interval=50)
+        a, inter = ctx.download()
+        out.append((got, a, inter, ctx.clock()))
+        ctx.close()
+    (g1, a1, i1, c1), (g0, a0_, i0, c0) = out
+    assert [(s["step"], s["time_ps"], s["mvv"]) for s in g1] == [(s["step"], s["time_ps"], s["mvv"]) for s in g0]
+    assert a1.tobytes() == a0_.tobytes() and i1.tobytes() == i0.tobytes() and c1 == c0
