@@ -1253,7 +1253,16 @@ static mg_status step_host_pipelined(mg_context *ctx, mg_atom_element *atoms, mg
     const int64_t plane = static_cast<int64_t>(g.Sx) * g.Sy;  // slots per z plane
     const size_t rec = sizeof(mg_atom_element);
     size_t ev = 0;
-    auto local_plane_bound = [&](int c) { return static_cast<int>((static_cast<int64_t>(c) * g.bz) / S); };
+    // copy-in chunks: uniform, but the last one thin (4 planes), since its unpack and firststep are not
+    // hidden behind a copy
+    auto local_plane_bound = [&](int c) {
+        if (S >= 3 && g.bz >= 8 * S) {
+            if (c == S) return g.bz;
+            if (c == S - 1) return g.bz - 4;
+            return static_cast<int>((static_cast<int64_t>(c) * (g.bz - 4)) / (S - 1));
+        }
+        return static_cast<int>((static_cast<int64_t>(c) * g.bz) / S);
+    };
 
     // in: the copies wait for everything already on the library stream
     MG_CK(cudaEventRecord(ctx->pipe_ev[ev], ctx->stream));
@@ -1320,10 +1329,15 @@ static mg_status step_host_pipelined(mg_context *ctx, mg_atom_element *atoms, mg
         launch_lat_force(lc, g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, true, mx, false);
         if ((st = flush(g.gz, g.Sz)) != MG_OK) return st;
     } else {
+        // slabs 0 .. 2 thin (4 planes): the first copy out waits for their density and slab 1's force
+        std::vector<int> kb(SS + 1);
+        const int thin = (SS >= 6 && g.bz >= 8 * SS) ? 3 : 0;
+        for (int c = 0; c <= SS; c++)
+            kb[c] = c <= thin ? 4 * c
+                              : 4 * thin + static_cast<int>((static_cast<int64_t>(c - thin) * (g.bz - 4 * thin)) / (SS - thin));
         std::vector<int> u(SS + 1);
         for (int c = 0; c <= SS; c++)
-            u[c] = c == SS ? g.n_local_half
-                           : static_cast<int>((((static_cast<int64_t>(c) * g.bz / SS) * per_plane) >> 5) << 5);
+            u[c] = c == SS ? g.n_local_half : static_cast<int>(((kb[c] * per_plane) >> 5) << 5);
         auto full_planes = [&](int c) { return c == SS ? g.bz : static_cast<int>(u[c] / per_plane); };  // below u[c]
         int df_done = 0;  // local planes whose in-plane ghosts have their df
         auto rho_slab = [&](int c) {

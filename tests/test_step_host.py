@@ -32,9 +32,10 @@ def _prepared_state(pkg, wl, cells, pot, precision, alloy=True):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("cells,chunks", [((11, 9, 13), 2), ((11, 9, 13), 5), ((11, 9, 13), 8), ((8, 10, 37), 8),
-                                          ((8, 10, 37), 16)])
+                                          ((8, 10, 37), 16), ((6, 6, 64), 8)])
 def test_pipelined_step_host_is_bit_identical(pkg, wl, potentials, gpu_lib, precision, cells, chunks):
-    """(11, 9, 13): 2 slabs (density unsplit) and 3 slabs; (8, 10, 37): 8 and 9 slabs of 4-5 planes."""
+    """(11, 9, 13): 2 slabs (density unsplit) and 3 slabs; (8, 10, 37): 8 and 9 slabs of 4-5 planes;
+    (6, 6, 64): thin first slabs and a thin last copy-in chunk."""
     a0, _ = _prepared_state(pkg, wl, cells, potentials["fecuni"], precision)
     got, want = a0.copy(), a0.copy()
     cp = _ctx(pkg, cells, potentials["fecuni"], precision, chunks)
