@@ -877,10 +877,10 @@ void launch_lat_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTab
 }
 
 // ------------------------------------------------------------------------------------------------
-// lattice force pass (atom::latForce, src/atom.cpp:311-358, as a full gather). When no inter or far
-// atom adds force afterwards, the second half-kick (NewtonMotion::secondstep,
-// src/newton_motion.cpp:57-67) is fused. fpair = -(F'_i rho'_j(r) + F'_j rho'_i(r) + phi'_ij(r)) / r,
-// phi = (r phi) / r.
+// lattice force pass (atom::latForce, src/atom.cpp:311-358, as a full gather). When no inter atom
+// adds force afterwards, the second half-kick (NewtonMotion::secondstep, src/newton_motion.cpp:57-67)
+// is fused, and inside a fused graph (mixed form) so is the next loop body's firststep.
+// fpair = -(F'_i rho'_j(r) + F'_j rho'_i(r) + phi'_ij(r)) / r, phi = (r phi) / r.
 // ------------------------------------------------------------------------------------------------
 template <int PAR>
 __device__ __forceinline__ void force_sum_fp64(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int sl, int ti,
@@ -1646,7 +1646,7 @@ void launch_inter_manage(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, 
 
 // ------------------------------------------------------------------------------------------------
 // inter-atom EAM (atom::interRho / interForce, src/atom.cpp:194-284, 360-473), FP64 arithmetic.
-// One thread per local inter atom; Newton-3 shares go to the owning lattice slot by FP64 atomics.
+// One warp per local inter atom; Newton-3 shares go to the owning lattice slot by FP64 atomics.
 // ------------------------------------------------------------------------------------------------
 __device__ __forceinline__ int bucket_begin(const Inter &in, int nb, int key) {
     int lo = 0, hi = nb;
