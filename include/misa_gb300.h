@@ -148,7 +148,8 @@ mg_status mg_dt_history(mg_context *ctx, double *out, int64_t cap, int64_t *n_ou
 mg_status mg_prepare(mg_context *ctx);
 /* nsteps iterations of the loop body (src/simulation.cpp:241-265): firststep, decide, exchangeInter,
  * borderInter, exchangeAtom, computeEam, secondstep. Asynchronous on the context stream unless
- * sync != 0. The step sequence is captured once as a CUDA graph and replayed. */
+ * sync != 0. The step sequence is captured once as a CUDA graph and replayed; in the mixed form with
+ * a fixed dt, runs of 16 bodies replay one fused graph (mg_set_step_fusion). */
 mg_status mg_simulate(mg_context *ctx, int64_t nsteps, int32_t sync);
 /* One phase of the loop body, for parity checks: 0 firststep, 1 decide, 2 exchangeInter,
  * 3 borderInter, 4 exchangeAtom, 5 computeEam, 6 secondstep. */

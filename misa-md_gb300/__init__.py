@@ -577,6 +577,22 @@ class Simulation:
     def simulate(self, steps):
         self.ctx.simulate(steps, sync=True)
 
+    def run_stages(self, stages, steps, default_dt, thermo_interval=0, dump_path=None, dump_interval=0,
+                   by_frame=False, origin_dump_path=None):
+        """MDSimulation's run (frontend/md_simulation.cpp:24-111): the stage list on the device, atom
+        frames every dump_interval steps into dump_path (OutputCopy; by_frame: one file per frame,
+        "{}" in the path), the state before each PKA into origin_dump_path, and the dump header written
+        at the end (onSimulationDone -> onAllOut). Returns the thermo samples."""
+        n = 2 * self.phase_space[0] * self.phase_space[1] * self.phase_space[2]
+        dump = self.ctx.dump_open(dump_path, by_frame=by_frame) if dump_path and dump_interval else None
+        try:
+            self.ctx.set_stage_output(dump, dump_interval if dump else 0, origin_dump_path)
+            return self.ctx.run_stages(stages, steps, default_dt, n, thermo_interval)
+        finally:
+            self.ctx.set_stage_output()
+            if dump is not None:
+                dump.close()
+
     def collision_step(self, coll_lat, coll_dir, pka_energy):
         self.ctx.collision_step(coll_lat, coll_dir, pka_energy)
 

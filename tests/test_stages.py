@@ -93,3 +93,20 @@ def test_stage_machine_fused_bodies_are_bit_identical(pkg, wl, potentials, gpu_l
     (g1, a1, i1, c1), (g0, a0_, i0, c0) = out
     assert [(s["step"], s["time_ps"], s["mvv"]) for s in g1] == [(s["step"], s["time_ps"], s["mvv"]) for s in g0]
     assert a1.tobytes() == a0_.tobytes() and i1.tobytes() == i0.tobytes() and c1 == c0
+
+
+def test_simulation_run_stages_with_dumps(pkg, wl, potentials, gpu_lib, tmp_path):
+    """The Simulation mirror runs a staged schedule with interval frames and an origin dump."""
+    sim = pkg.Simulation(precision="mixed")
+    sim.create_domain((8, 8, 8), A0, RCF)
+    sim.create_atoms(0.001, 300.0, 7)
+    sim.prepare_for_start(potentials["fe"])
+    stages = [{"steps": 40, "step_length": 0.0005},
+              {"steps": 24, "collision_step": 5, "lat": [4, 4, 4, 0], "direction": [1.0, 1.0, 2.0], "energy": 100.0}]
+    out = sim.run_stages(stages, 64, 0.001, thermo_interval=16, dump_path=str(tmp_path / "run.out"), dump_interval=32,
+                         origin_dump_path=str(tmp_path / "origin.out"))
+    assert [s["step"] for s in out] == [16, 32, 48, 64]
+    frames = pkg.dumpfile.frames(str(tmp_path / "run.out"))
+    assert sorted(frames) == [32, 64] and all(f.size == 2 * 8 ** 3 for f in frames.values())
+    origin = pkg.dumpfile.read(str(tmp_path / "origin.out"))
+    assert origin.size == 2 * 8 ** 3 and set(origin["step"].tolist()) == {44}
