@@ -460,6 +460,7 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     const int cut_lattice = static_cast<int>(std::ceil(rcf));      // libcomm cut_lattice
     for (int d = 0; d < 3; d++) {
         if (phase_space[d] < 2 * ghost) { g_create_error = "every dimension needs at least 2*ghost unit cells"; return MG_ERR_ARG; }
+        if (phase_space[d] > (1 << 20)) { g_create_error = "box too large for 32-bit slot indices"; return MG_ERR_ARG; }
     }
     const int64_t Sx = 2 * (phase_space[0] + 2 * ghost), Sy = phase_space[1] + 2 * ghost, Sz = phase_space[2] + 2 * ghost;
     if (Sx * Sy * Sz >= (int64_t) 0x7fffffff - 1024) { g_create_error = "box too large for 32-bit slot indices"; return MG_ERR_ARG; }

@@ -387,6 +387,10 @@ def test_bad_inputs_are_rejected(pkg, wl, potentials, gpu_lib, tmp_path):
         ctx.prepare()
     with pytest.raises(pkg.MgError):
         pkg.Context((4, 6, 6), A0, RCF)  # narrower than 2 ghost widths
+    with pytest.raises(pkg.MgError):
+        pkg.Context((1300, 1300, 1300), A0, RCF)  # more slots than 32-bit indices address
+    with pytest.raises(pkg.MgError):
+        pkg.Context((6, 6, 1 << 40), A0, RCF)
     ctx.close()
 
 
