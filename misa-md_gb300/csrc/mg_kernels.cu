@@ -1051,7 +1051,10 @@ __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables 
     const double fx = h * (double) sx;
     const double fy = h * (double) sy;
     const double fz = h * (double) sz;
-    s.fx[sl] = fx; s.fy[sl] = fy; s.fz[sl] = fz;
+    const bool fused = fuse_next && kick && !hook && lattice_only(in);
+    // a fused body's forces are used only in registers: the next body's firststep is taken here, and
+    // the last body of a graph (never fused) stores the forces the state keeps between launches
+    if (!fused) { s.fx[sl] = fx; s.fy[sl] = fy; s.fz[sl] = fz; }
     if (kick && !hook && lattice_only(in)) {
         const double c = dt_inv_m_of(sp, ti);
         const double vx = __dadd_rn(s.vx[sl], __dmul_rn(c, fx));
