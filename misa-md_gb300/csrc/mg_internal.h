@@ -18,7 +18,8 @@ constexpr double kFtm2v = (1.0 / kMvv2e);    // src/types/pre_define.h:19
 constexpr double kNeiLatCutoff = 0.5;        // src/md_building_config.h.in:24
 constexpr int kMaxFull = 232;
 constexpr int kFirstThreads = 256;           // firststep block = one group of displaced flags (8 per lane)
-constexpr int kSortSmemKeys = 16384;         // bucket keys the list manager sorts in shared memory                // capacity of a full offset table per parity
+constexpr int kSortSmemKeys = 16384;
+constexpr int kVoteWords = 4;                // vote bits per 32-site group: pruned candidates up to 128         // bucket keys the list manager sorts in shared memory                // capacity of a full offset table per parity
 
 // box flags (src/lattice/box.h:12-20)
 constexpr uint32_t kInBox = 0, kXLow = 1u, kXHigh = 2u, kYLow = 4u, kYHigh = 8u, kZLow = 16u, kZHigh = 32u;
@@ -83,6 +84,7 @@ struct Slots {
     // mixed form, parity-split layout (slot s at (s & 1) * half + (s >> 1)):
     float4 *u4;              // displacement from the site in half-lattice units, w = type bits
     float4 *u4n;             // the next loop body's u4 buffer when the force pass takes the next firststep
+    unsigned *umask;         // per 32-site group and parity: kVoteWords words of votes on the pruned candidates
     float *df32;             // F'(rho) in float
 };
 
@@ -236,9 +238,14 @@ void launch_far_clear(const LaunchCtx &lc, const Geom &g, Inter in);
 void launch_far_mark(const LaunchCtx &lc, const Geom &g, Inter in);
 void launch_ghost_copy(const LaunchCtx &lc, const Geom &g, Slots s, bool mixed);
 void launch_ghost_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool mixed);
-void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook);
+// votes (mixed form): leave, per 32-site group, which pruned candidates any site has inside the
+// cutoff, for the force pass of the same step (when votes_ok; the force pass must get the same flag)
+void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook,
+                    bool votes = false);
 // the density pass over the sites [u0, u1) of both parities (as launch_lat_force_sites)
-void launch_lat_rho_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, int u0, int u1);
+void launch_lat_rho_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, int u0, int u1,
+                          bool votes = false);
+bool votes_ok(const LaunchCtx &lc, const Geom &g);
 // forward df for the ghost slots inside local planes [k0, k1), or (k0 < 0) the ghost planes below and
 // above the box plus the ghost inter atoms
 void launch_ghost_df_planes(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool mixed, int k0, int k1);
@@ -246,11 +253,11 @@ void launch_lat_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTab
 // fuse_next (mixed form, kick, fixed dt): after the second half-kick each lattice atom also takes the
 // next step's firststep (into u4n), when no inter atoms exist
 void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *sp, bool kick,
-                      bool mixed, bool hook, bool fuse_next = false);
+                      bool mixed, bool hook, bool fuse_next = false, bool votes = false);
 // the force pass over the sites of both parities whose index within their parity is in [u0, u1):
 // with u0 and u1 multiples of 32 (or u1 = n_local_half) the slabs of a split pass are disjoint warps
 void launch_lat_force_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *sp, bool kick,
-                            bool mixed, int u0, int u1);
+                            bool mixed, int u0, int u1, bool votes = false);
 void launch_secondstep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams *sp, bool lattice);
 // step head: records the step's dt and, in variable mode, sets dt from the last kick's max |v|
 void launch_step_head(const LaunchCtx &lc, StepParams *sp);

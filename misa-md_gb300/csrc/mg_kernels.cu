@@ -42,8 +42,7 @@ __device__ __forceinline__ int sidx(const Geom &g, int s) { return (s & 1) * g.h
 // each run of 64 threads covers 32 consecutive even sites (first warp) and the 32 odd sites beside
 // them (second warp), so both halves of each output sector are written close in time. The
 // autotuner picks per kernel. Returns -1 past the end.
-__device__ __forceinline__ int gather_slot(const Geom &g, int t, int order, int &par) {
-    int u;
+__device__ __forceinline__ int gather_site(const Geom &g, int t, int order, int &par, int &u) {
     if (order) {
         par = (t >> 5) & 1;
         u = ((t >> 6) << 5) | (t & 31);  // index among the sites of this parity
@@ -55,6 +54,10 @@ __device__ __forceinline__ int gather_slot(const Geom &g, int t, int order, int 
     const int ih = u % g.nxh;
     const int r = u / g.nxh;
     return lin(g, 2 * ih + par + g.gx, r % g.by + g.gy, r / g.by + g.gz);
+}
+__device__ __forceinline__ int gather_slot(const Geom &g, int t, int order, int &par) {
+    int u;
+    return gather_site(g, t, order, par, u);
 }
 // threads to launch for the gathers
 inline int gather_threads(const Geom &g, int order) {
@@ -750,44 +753,94 @@ __global__ void __launch_bounds__(512) k_lat_rho_fp64(const __grid_constant__ Ne
     for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x) k_lat_rho_fp64_site(t, nt, g, s, in, pt, hook, order);
 }
 
+// r^2 of a candidate pair in half-lattice units (and the pair vector), each operation rounded as
+// written: the density and force passes both compute it and must agree bit for bit on which pairs
+// lie inside the cutoff (the force pass skips the tail candidates no site of a group had inside)
+__device__ __forceinline__ float pair_r2(f2 uixy, float uiz, float4 D, float4 uj, f2 &dxy, float &dz) {
+    dxy = f2_sub(f2_sub(uixy, f2_pack(uj.x, uj.y)), f2_pack(D.x, D.y));
+    dz = __fsub_rn(__fsub_rn(uiz, uj.z), D.z);
+    float dx, dy;
+    f2_unpack(dxy, dx, dy);
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+// one density term (in range): rho_tj(r)
+__device__ __forceinline__ void rho_pair(const PotTables &pt, float r2, float4 uj, float &sum, float &comp) {
+    const int tj = __float_as_int(uj.w);
+    const float rp = r2 * rsqrtf(r2);
+    int m; float p;
+    locate_r_f(rp, pt.h_inv_dr_f, pt.nr, m, p);
+    kahan(sum, comp, val_f(pt.rho_vf + tj * pt.nr, m, p));
+}
 template <int PAR>
 __device__ __forceinline__ void rho_sum_mixed(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int si, float4 ui,
                                               int q0, int q1, float &sum, float &comp) {
     const float rc2 = g.rc2_h;
-    const float hinv = pt.h_inv_dr_f;
-    const int nr = pt.nr;
     const f2 uixy = f2_pack(ui.x, ui.y);
 #pragma unroll 2  // 1, 4 and 8 measured slower
     for (int q = q0; q < q1; q++) {
         const float4 D = nt.cand[PAR][q];
         const float4 uj = __ldg(s.u4 + si + __float_as_int(D.w));
-        const f2 dxy = f2_sub(f2_sub(uixy, f2_pack(uj.x, uj.y)), f2_pack(D.x, D.y));
-        const float dz = (ui.z - uj.z) - D.z;
-        float dx, dy;
-        f2_unpack(dxy, dx, dy);
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 < rc2) {  // false for vacancies (NaN coordinates)
-            const int tj = __float_as_int(uj.w);
-            const float rp = r2 * rsqrtf(r2);
-            int m; float p;
-            locate_r_f(rp, hinv, nr, m, p);
-            kahan(sum, comp, val_f(pt.rho_vf + tj * nr, m, p));
-        }
+        f2 dxy; float dz;
+        const float r2 = pair_r2(uixy, ui.z, D, uj, dxy, dz);
+        if (r2 < rc2) rho_pair(pt, r2, uj, sum, comp);  // false for vacancies (NaN coordinates)
     }
 }
+// the pruned candidates [q0, q1), q1 - q0 <= 32, noting which this site has inside the cutoff (bit j:
+// candidate q0 + j). The bit is set inside the in-range branch, so the notes cost next to nothing.
+// FULL: q1 - q0 is 32, known at compile time (the full chunks; a runtime count there costs registers).
+template <int PAR, bool FULL>
+__device__ __forceinline__ unsigned rho_sum_noted(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt,
+                                                  int si, float4 ui, int q0, int q1, float &sum, float &comp) {
+    const float rc2 = g.rc2_h;
+    const f2 uixy = f2_pack(ui.x, ui.y);
+    unsigned bits = 0;
+#pragma unroll 2
+    for (int j = 0; j < (FULL ? 32 : q1 - q0); j++) {
+        const float4 D = nt.cand[PAR][q0 + j];
+        const float4 uj = __ldg(s.u4 + si + __float_as_int(D.w));
+        f2 dxy; float dz;
+        const float r2 = pair_r2(uixy, ui.z, D, uj, dxy, dz);
+        if (r2 < rc2) {
+            rho_pair(pt, r2, uj, sum, comp);
+            bits |= 1u << j;
+        }
+    }
+    return bits;
+}
+__device__ __forceinline__ unsigned *group_words(const Geom &g, const Slots &s, int par, int u) {
+    return s.umask + kVoteWords * (par * ((g.n_local_half + 31) >> 5) + (u >> 5));
+}
 
-__device__ __forceinline__ void k_lat_rho_mixed_site(int t, const NeighTables &nt, const Geom &g, const Slots &s, const Inter &in, const PotTables &pt, bool hook, int order) {
-    int par;
-    const int sl = gather_slot(g, t, order, par);
-    if (sl < 0) return;
-    const int si = sidx(g, sl);
-    const float4 ui = s.u4[si];
+// votes: write the group words of the pruned tail (all 32 lanes of the warp call this, with valid
+// false for threads past the end; the warp covers one 32-site group of one parity)
+__device__ __forceinline__ void k_lat_rho_mixed_site(int t, bool valid, const NeighTables &nt, const Geom &g, const Slots &s, const Inter &in,
+                                                     const PotTables &pt, bool hook, int order, bool votes) {
+    int par = 0, u = 0;
+    const int sl = valid ? gather_site(g, t, order, par, u) : -1;
+    const int si = sl >= 0 ? sidx(g, sl) : 0;
+    const float4 ui = sl >= 0 ? s.u4[si] : vacant_u4();
     const int ti = __float_as_int(ui.w);
+    const unsigned live = votes ? __ballot_sync(0xffffffffu, ti >= 0) : 0u;
+    if (sl < 0) return;
     if (ti < 0) { s.rho[sl] = 0.0; return; }
     float sum = 0.f, comp = 0.f;
     const int np = nt.npruned;
-    if (par) rho_sum_mixed<1>(nt, g, s, pt, si, ui, 0, np, sum, comp);
-    else rho_sum_mixed<0>(nt, g, s, pt, si, ui, 0, np, sum, comp);
+    if (votes) {  // 32 candidates per vote word; the group's word: any live site of the warp
+        unsigned *w = group_words(g, s, par, u);
+        const bool leader = (int) (threadIdx.x & 31) == __ffs(live) - 1;
+        for (int k = 0; k * 32 < np; k++) {
+            const int q0 = 32 * k, q1 = min(q0 + 32, np);
+            const unsigned bits = q1 - q0 == 32 ? (par ? rho_sum_noted<1, true>(nt, g, s, pt, si, ui, q0, q1, sum, comp)
+                                                       : rho_sum_noted<0, true>(nt, g, s, pt, si, ui, q0, q1, sum, comp))
+                                                : (par ? rho_sum_noted<1, false>(nt, g, s, pt, si, ui, q0, q1, sum, comp)
+                                                       : rho_sum_noted<0, false>(nt, g, s, pt, si, ui, q0, q1, sum, comp));
+            const unsigned any = __reduce_or_sync(live, bits);
+            if (leader) w[k] = any;
+        }
+    } else {
+        if (par) rho_sum_mixed<1>(nt, g, s, pt, si, ui, 0, np, sum, comp);
+        else rho_sum_mixed<0>(nt, g, s, pt, si, ui, 0, np, sum, comp);
+    }
     if (in.far_flag[sl]) {
         const int nf = nt.nfull;
         if (par) rho_sum_mixed<1>(nt, g, s, pt, si, ui, np, nf, sum, comp);
@@ -801,34 +854,44 @@ __device__ __forceinline__ void k_lat_rho_mixed_site(int t, const NeighTables &n
         s.df32[si] = der_f(pt.F_dff + ti * pt.nrho, m, p);
     }
 }
-template <bool LOOP>  // LOOP: several sites per thread, one grid stride apart
-__global__ void __launch_bounds__(512) k_lat_rho_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool hook, int order, int tbase,
-                                                       int nthreads) {
+template <bool LOOP>  // LOOP: several sites per thread, one grid stride apart (no votes)
+__global__ void __launch_bounds__(512, 4) k_lat_rho_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool hook, int order, int tbase,
+                                                       int nthreads, bool votes) {
     const int t0 = tbase + blockIdx.x * blockDim.x + threadIdx.x;  // threads [tbase, nthreads)
     if (!LOOP) {
-        if (t0 < nthreads) k_lat_rho_mixed_site(t0, nt, g, s, in, pt, hook, order);
+        k_lat_rho_mixed_site(t0, t0 < nthreads, nt, g, s, in, pt, hook, order, votes);
         return;
     }
-    for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x) k_lat_rho_mixed_site(t, nt, g, s, in, pt, hook, order);
+    for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x)
+        k_lat_rho_mixed_site(t, true, nt, g, s, in, pt, hook, order, false);
 }
 
 // atoms per thread: each thread takes rho_apt sites, one grid stride apart (the stride is a multiple
 // of 64, so warps keep their parity and thread order)
+// The density pass can leave per-group votes on the pruned candidates for the force pass of the same
+// step when every warp of both passes covers one 32-site group of one parity: one site per thread, and
+// (for the parity-major order) a multiple of 32 sites per parity; the candidates fit the vote words.
+bool votes_ok(const LaunchCtx &lc, const Geom &g) {
+    const bool aligned = (g.n_local_half & 31) == 0;
+    return lc.nt->npruned <= 32 * kVoteWords && lc.rho_apt == 1 && lc.force_apt == 1 && (lc.rho_order == 1 || aligned) &&
+           (lc.force_order == 1 || aligned);
+}
 static void launch_lat_rho_threads(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook,
-                                   int tb, int te) {
+                                   int tb, int te, bool votes = false) {
     const int order = lc.rho_order, b = lc.rho_block;
     const int n = (te - tb + b * lc.rho_apt - 1) / (b * lc.rho_apt);
     if (n <= 0) return;
     if (lc.rho_apt > 1) {
-        if (mixed) k_lat_rho_mixed<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, tb, te);
+        if (mixed) k_lat_rho_mixed<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, tb, te, false);
         else k_lat_rho_fp64<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, tb, te);
     } else {
-        if (mixed) k_lat_rho_mixed<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, tb, te);
+        if (mixed) k_lat_rho_mixed<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, tb, te, votes);
         else k_lat_rho_fp64<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, tb, te);
     }
 }
-void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook) {
-    launch_lat_rho_threads(lc, g, s, in, t, mixed, hook, 0, gather_threads(g, lc.rho_order));
+void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook, bool votes) {
+    launch_lat_rho_threads(lc, g, s, in, t, mixed, hook, 0, gather_threads(g, lc.rho_order),
+                           votes && mixed && !hook && votes_ok(lc, g));
 }
 // thread range of the sites [u0, u1) of both parities (u0, u1 multiples of 32, or u1 = n_local_half)
 static void site_threads(const Geom &g, int order, int u0, int u1, int tb[2], int te[2], int &nr) {
@@ -842,11 +905,13 @@ static void site_threads(const Geom &g, int order, int u0, int u1, int tb[2], in
         nr = 2;
     }
 }
-void launch_lat_rho_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, int u0, int u1) {
+void launch_lat_rho_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, int u0, int u1,
+                          bool votes) {
     if (u1 <= u0) return;
     int tb[2], te[2], nr;
     site_threads(g, lc.rho_order, u0, u1, tb, te, nr);
-    for (int r = 0; r < nr; r++) launch_lat_rho_threads(lc, g, s, in, t, mixed, false, tb[r], te[r]);
+    const bool v = votes && mixed && votes_ok(lc, g);
+    for (int r = 0; r < nr; r++) launch_lat_rho_threads(lc, g, s, in, t, mixed, false, tb[r], te[r], v);
 }
 
 // dF/drho when inter atoms added density after the lattice pass (or for the df hook)
@@ -960,6 +1025,43 @@ __global__ void __launch_bounds__(512) k_lat_force_fp64(const __grid_constant__ 
     for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x) k_lat_force_fp64_site(t, nt, g, s, in, pt, sp, kick, hook, order);
 }
 
+// one candidate of the force pass: the pair term when inside the cutoff (false for vacancies, NaN)
+template <int PAR>
+__device__ __forceinline__ void force_candidate(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int si,
+                                                int ti, int fbase, f2 uixy, float uiz, float dfi, int q, f2 &sxy, float &sz) {
+    const float4 D = nt.cand[PAR][q];
+    const int oj = si + __float_as_int(D.w);
+    const float4 uj = __ldg(s.u4 + oj);
+    f2 dxy; float dz;
+    const float r2 = pair_r2(uixy, uiz, D, uj, dxy, dz);
+    if (r2 < g.rc2_h) {
+        const int tj = __float_as_int(uj.w);
+        const float rinv_h = rsqrtf(r2);
+        const float rp = r2 * rinv_h;
+        int m; float p;
+        locate_r_f(rp, pt.h_inv_dr_f, pt.nr, m, p);
+        // record {c0, d0, c1, d1, c2, d2, c3, 0}: r*phi = c(p), rho_tj' = d(p), both in one Horner
+        float z[8];
+        ld_nc_v8(pt.zr8 + 8 * (fbase + tj * pt.nr + m), z);
+        const f2 pp = f2_pack(p, p);
+        f2 h = f2_fma(f2_pack(z[6], z[7]), pp, f2_pack(z[4], z[5]));
+        h = f2_fma(h, pp, f2_pack(z[2], z[3]));
+        h = f2_fma(h, pp, f2_pack(z[0], z[1]));
+        float zv, rhojp;
+        f2_unpack(h, zv, rhojp);
+        const float zp = fmaf(fmaf(3.0f * z[6], p, z[4] + z[4]), p, z[2]) * pt.inv_dr_f;
+        const float rhoip = (tj == ti) ? rhojp : der_f(pt.rho_dff + ti * pt.nr, m, p);
+        const float rinv = rinv_h * g.inv_h_f;
+        const float phi = zv * rinv;
+        const float phip = (zp - phi) * rinv;
+        const float psip = dfi * rhojp + __ldg(s.df32 + oj) * rhoip + phip;
+        const float fpair = -psip * rinv;
+        // plain FP32 accumulation: compensating it changed the force error by less than 1e-7 eV/A
+        // RMS and cost 7% of the pass
+        sxy = f2_fma(dxy, f2_pack(fpair, fpair), sxy);
+        sz = fmaf(dz, fpair, sz);
+    }
+}
 template <int PAR>
 __device__ __forceinline__ void force_sum_mixed(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int si, int ti,
                                                 float4 ui, float dfi, int q0, int q1, f2 &sxy, float &sz) {
@@ -967,43 +1069,18 @@ __device__ __forceinline__ void force_sum_mixed(const NeighTables &nt, const Geo
     const int fbase = (ti * 3) * pt.nr;
     const f2 uixy = f2_pack(ui.x, ui.y);
 #pragma unroll 1  // 2, 3, 4 and full unrolling measured slower
-    for (int q = q0; q < q1; q++) {
-        const float4 D = nt.cand[PAR][q];
-        const int oj = si + __float_as_int(D.w);
-        const float4 uj = __ldg(s.u4 + oj);
-        const f2 dxy = f2_sub(f2_sub(uixy, f2_pack(uj.x, uj.y)), f2_pack(D.x, D.y));
-        const float dz = (ui.z - uj.z) - D.z;
-        float dx, dy;
-        f2_unpack(dxy, dx, dy);
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 < g.rc2_h) {  // false for vacancies (NaN coordinates)
-            const int tj = __float_as_int(uj.w);
-            const float rinv_h = rsqrtf(r2);
-            const float rp = r2 * rinv_h;
-            int m; float p;
-            locate_r_f(rp, pt.h_inv_dr_f, pt.nr, m, p);
-            // record {c0, d0, c1, d1, c2, d2, c3, 0}: r*phi = c(p), rho_tj' = d(p), both in one Horner
-            float z[8];
-            ld_nc_v8(pt.zr8 + 8 * (fbase + tj * pt.nr + m), z);
-            const f2 pp = f2_pack(p, p);
-            f2 h = f2_fma(f2_pack(z[6], z[7]), pp, f2_pack(z[4], z[5]));
-            h = f2_fma(h, pp, f2_pack(z[2], z[3]));
-            h = f2_fma(h, pp, f2_pack(z[0], z[1]));
-            float zv, rhojp;
-            f2_unpack(h, zv, rhojp);
-            const float zp = fmaf(fmaf(3.0f * z[6], p, z[4] + z[4]), p, z[2]) * pt.inv_dr_f;
-            const float rhoip = (tj == ti) ? rhojp : der_f(pt.rho_dff + ti * pt.nr, m, p);
-            const float rinv = rinv_h * g.inv_h_f;
-            const float phi = zv * rinv;
-            const float phip = (zp - phi) * rinv;
-            const float psip = dfi * rhojp + __ldg(s.df32 + oj) * rhoip + phip;
-            const float fpair = -psip * rinv;
-            // plain FP32 accumulation: compensating it changed the force error by less than 1e-7 eV/A
-            // RMS and cost 7% of the pass
-            sxy = f2_fma(dxy, f2_pack(fpair, fpair), sxy);
-            sz = fmaf(dz, fpair, sz);
-        }
-    }
+    for (int q = q0; q < q1; q++) force_candidate<PAR>(nt, g, s, pt, si, ti, fbase, uixy, ui.z, dfi, q, sxy, sz);
+}
+// the pruned candidates the density pass of this step found inside the cutoff for some site of the
+// warp's group, in table order (the others are outside for every site: same displacements, same r^2)
+template <int PAR>
+__device__ __forceinline__ void force_sum_voted(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int si,
+                                                int ti, float4 ui, float dfi, const unsigned *words, f2 &sxy, float &sz) {
+    const int fbase = (ti * 3) * pt.nr;
+    const f2 uixy = f2_pack(ui.x, ui.y);
+    for (int k = 0; k * 32 < nt.npruned; k++)
+        for (unsigned w = words[k]; w; w &= w - 1)
+            force_candidate<PAR>(nt, g, s, pt, si, ti, fbase, uixy, ui.z, dfi, 32 * k + __ffs(w) - 1, sxy, sz);
 }
 
 // local coordinates and local index (k, j, i order) of a local slot
@@ -1017,9 +1094,9 @@ __device__ __forceinline__ int local_index_of(const Geom &g, int sl, int &i, int
 
 __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables &nt, const Geom &g, const Slots &s, const Inter &in,
                                                 const PotTables &pt, StepParams *sp, bool kick, bool hook, int order,
-                                                bool fuse_next) {
-    int par;
-    const int sl = gather_slot(g, t, order, par);
+                                                bool fuse_next, bool votes) {
+    int par, u;
+    const int sl = gather_site(g, t, order, par, u);
     if (sl < 0) return;
     const int si = sidx(g, sl);
     const float4 ui = s.u4[si];
@@ -1038,8 +1115,14 @@ __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables 
     f2 sxy = f2_pack(0.f, 0.f);
     float sz = 0.f;
     const int np = nt.npruned;
-    if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, 0, np, sxy, sz);
-    else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, 0, np, sxy, sz);
+    if (votes) {  // the density pass of this step left the votes of this warp's group
+        const unsigned *w = group_words(g, s, par, u);
+        if (par) force_sum_voted<1>(nt, g, s, pt, si, ti, ui, dfi, w, sxy, sz);
+        else force_sum_voted<0>(nt, g, s, pt, si, ti, ui, dfi, w, sxy, sz);
+    } else {
+        if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, 0, np, sxy, sz);
+        else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, 0, np, sxy, sz);
+    }
     if (in.far_flag[sl]) {
         const int nf = nt.nfull;
         if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, np, nf, sxy, sz);
@@ -1075,40 +1158,43 @@ __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables 
 template <bool LOOP>  // LOOP: several sites per thread, one grid stride apart
 __global__ void __launch_bounds__(512, 3) k_lat_force_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt,
                                                          StepParams *sp, bool kick, bool hook, int order, int tbase,
-                                                         int nthreads, bool fuse_next) {
+                                                         int nthreads, bool fuse_next, bool votes) {
     const int t0 = tbase + blockIdx.x * blockDim.x + threadIdx.x;  // threads [tbase, nthreads)
     if (!LOOP) {
-        if (t0 < nthreads) k_lat_force_mixed_site(t0, nt, g, s, in, pt, sp, kick, hook, order, fuse_next);
+        if (t0 < nthreads) k_lat_force_mixed_site(t0, nt, g, s, in, pt, sp, kick, hook, order, fuse_next, votes);
         return;
     }
     for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x)
-        k_lat_force_mixed_site(t, nt, g, s, in, pt, sp, kick, hook, order, fuse_next);
+        k_lat_force_mixed_site(t, nt, g, s, in, pt, sp, kick, hook, order, fuse_next, false);
 }
 
 static void launch_lat_force_threads(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *p,
-                                     bool kick, bool mixed, bool hook, int tb, int te, bool fuse_next = false) {
+                                     bool kick, bool mixed, bool hook, int tb, int te, bool fuse_next = false,
+                                     bool votes = false) {
     const int order = lc.force_order, b = lc.force_block;
     const int n = (te - tb + b * lc.force_apt - 1) / (b * lc.force_apt);
     if (n <= 0) return;
     const bool fuse = fuse_next && mixed && kick && !hook;
     if (lc.force_apt > 1) {
-        if (mixed) k_lat_force_mixed<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te, fuse);
+        if (mixed) k_lat_force_mixed<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te, fuse, false);
         else k_lat_force_fp64<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te);
     } else {
-        if (mixed) k_lat_force_mixed<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te, fuse);
+        if (mixed) k_lat_force_mixed<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te, fuse, votes);
         else k_lat_force_fp64<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te);
     }
 }
 void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *p, bool kick,
-                      bool mixed, bool hook, bool fuse_next) {
-    launch_lat_force_threads(lc, g, s, in, t, p, kick, mixed, hook, 0, gather_threads(g, lc.force_order), fuse_next);
+                      bool mixed, bool hook, bool fuse_next, bool votes) {
+    launch_lat_force_threads(lc, g, s, in, t, p, kick, mixed, hook, 0, gather_threads(g, lc.force_order), fuse_next,
+                             votes && mixed && !hook && votes_ok(lc, g));
 }
 void launch_lat_force_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *p, bool kick,
-                            bool mixed, int u0, int u1) {
+                            bool mixed, int u0, int u1, bool votes) {
     if (u1 <= u0) return;
     int tb[2], te[2], nr;
     site_threads(g, lc.force_order, u0, u1, tb, te, nr);
-    for (int r = 0; r < nr; r++) launch_lat_force_threads(lc, g, s, in, t, p, kick, mixed, false, tb[r], te[r]);
+    const bool v = votes && mixed && votes_ok(lc, g);
+    for (int r = 0; r < nr; r++) launch_lat_force_threads(lc, g, s, in, t, p, kick, mixed, false, tb[r], te[r], false, v);
 }
 
 // second half-kick for lattice slots (only when inter atoms prevented fusion, or always) and for
