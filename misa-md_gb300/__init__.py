@@ -125,6 +125,8 @@ _PROTOS = {
     "mg_set_stage_output": (_I32, [_P, _P, _U64, ctypes.c_char_p]),
     "mg_set_host_pipeline": (_I32, [_P, _I32]),
     "mg_set_step_fusion": (_I32, [_P, _I32]),
+    "mg_set_neighbour_skin": (_I32, [_P, ctypes.c_double]),
+    "mg_skin_stats": (_I32, [_P, _P, _P]),
 }
 
 
@@ -401,6 +403,16 @@ class Context:
     def set_step_fusion(self, steps_per_graph):
         """Loop bodies per graph launch of simulate in the mixed form (fused firststep; 0 or 1: off)."""
         self._check(self.lib.mg_set_step_fusion(self.h, int(steps_per_graph)))
+
+    def set_neighbour_skin(self, skin):
+        """Verlet skin (Angstrom) of the mixed form's candidate lists (0: off); results do not depend on it."""
+        self._check(self.lib.mg_set_neighbour_skin(self.h, float(skin)))
+
+    def skin_stats(self):
+        """(density passes that used the candidate lists, passes that rebuilt them)."""
+        p, r = ctypes.c_int64(0), ctypes.c_int64(0)
+        self._check(self.lib.mg_skin_stats(self.h, ctypes.byref(p), ctypes.byref(r)))
+        return p.value, r.value
 
     def set_host_pipeline(self, chunks):
         """z-slabs of step_host's copy/compute pipeline (0 or 1: off)."""

@@ -74,6 +74,7 @@ struct mg_context {
     int fuse_steps = 16;
     cudaGraphExec_t graph_multi = nullptr;
     float4 *u4_main = nullptr, *u4_alt = nullptr;  // s.u4 and s.u4n outside fused graphs
+    bool alt_bodies = false;        // capturing bodies that alternate u4 buffers
     bool graph_stale = true;
     uint64_t gen = 1;               // bumped whenever captured graphs of this context go stale
     int graph_prec = -1;
@@ -130,6 +131,16 @@ cudaError_t dalloc(mg_context *ctx, T **p, size_t n) {
     return e;
 }
 
+// Verlet skin of the near words (mixed form), Angstrom. The group lists then hold about the sixth
+// shell besides the 58 neighbours inside the cutoff; at 600 K and dt = 1 fs they last about 10 steps
+// (0.2 to 0.3 A measured equally fast on 16M atoms).
+constexpr double kDefaultSkin = 0.25;
+void set_skin(Geom &g, double skin) {
+    g.skin_h = static_cast<float>(skin * g.inv_h);
+    const double r = (g.rc + skin) * g.inv_h;
+    g.rcs2_h = skin > 0.0 ? static_cast<float>(r * r) : g.rc2_h;
+}
+
 int next_pow2(int n) {
     int p = 1;
     while (p < n) p <<= 1;
@@ -168,7 +179,7 @@ struct Timer {
 // ---- the kernel sequences ----
 void seq_firststep(mg_context *ctx, bool decide, Timer *t, bool fused = false) {
     const LaunchCtx lc = ctx->lc();
-    launch_firststep(lc, ctx->g, ctx->s, ctx->in, ctx->d_sp, decide, 0, -1, fused);
+    launch_firststep(lc, ctx->g, ctx->s, ctx->in, ctx->d_sp, decide, 0, -1, fused, ctx->alt_bodies);
     if (t) t->mark(1);
     launch_inter_firststep(lc, ctx->in, ctx->d_sp);
     if (t) t->mark(2);
@@ -229,7 +240,7 @@ void seq_step(mg_context *ctx, Timer *t, bool fused_prev = false, bool fuse_next
 }
 // steps of mg_simulate that run fused: the mixed form with a fixed dt
 bool fusable(const mg_context *ctx) { return ctx->fuse_steps >= 2 && ctx->mixed() && ctx->dx_max <= 0.0; }
-constexpr int kLaunchesPerStep = 17;
+constexpr int kLaunchesPerStep = 18;
 
 mg_status require_ready(mg_context *ctx) {
     if (!ctx->pot_ready) { ctx->err = "potential not initialised"; return MG_ERR_POTENTIAL; }
@@ -409,10 +420,12 @@ mg_status build_graph_multi(mg_context *ctx) {
     cudaGraph_t graph;
     MG_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     const int k = ctx->fuse_steps;
+    ctx->alt_bodies = true;
     for (int i = 0; i < k; i++) {
         set_body_buffers(ctx, k, i);
         seq_step(ctx, nullptr, i > 0, i < k - 1);
     }
+    ctx->alt_bodies = false;
     set_body_buffers(ctx, k, k - 1);
     MG_CK(cudaStreamEndCapture(ctx->stream, &graph));
     cudaError_t e = cudaGraphInstantiate(&ctx->graph_multi, graph, 0);
@@ -491,6 +504,7 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     g.thr_lo_f = (float) (g.thr * (1.0 - 1e-4));
     g.rc2_h = (float) (g.rc2 * g.inv_h * g.inv_h);
     g.rc2_pre = (float) ((double) g.rc2_h * (1.0 + 1e-4));
+    set_skin(g, kDefaultSkin);
 
     // offset tables, and the lattice gather order: pruned entries (site distance below
     // rc + 0.4 a0, with margin) first, in reference order, then the rest
@@ -536,6 +550,8 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     ALLOC(s.type, ns); ALLOC(s.id, ns);
     ALLOC(s.u4, ns); ALLOC(s.u4n, ns); ALLOC(s.df32, ns);
     ALLOC(s.umask, static_cast<size_t>(2 * kVoteWords * ((g.n_local_half + 31) / 32)));
+    ALLOC(s.near, static_cast<size_t>(2 * kVoteWords * ((g.n_local_half + 31) / 32)));
+    ALLOC(s.skin, 1);
     ctx->u4_main = s.u4;
     ctx->u4_alt = s.u4n;
 
@@ -588,6 +604,8 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     if (e == cudaSuccess) e = cudaMemsetAsync(s.u4, 0xff, ns * sizeof(float4), ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s.u4n, 0xff, ns * sizeof(float4), ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_sp, 0, sizeof(StepParams), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s.skin, 0, sizeof(SkinState), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(&s.skin->dirty, 1, 1, ctx->stream);
     if (e != cudaSuccess) return fail(e);
     if (upload_tables(ctx) != MG_OK) { g_create_error = ctx->err; mg_destroy(ctx); return MG_ERR_CUDA; }
     launch_site_table(ctx->lc(), ctx->g, const_cast<double *>(ctx->g.site_half));
@@ -920,8 +938,10 @@ mg_status mg_simulate(mg_context *ctx, int64_t nsteps, int32_t sync) {
             const bool in_block = i < blocks * k;
             const int64_t pos = i % k;
             if (in_block) set_body_buffers(ctx, k, pos);
+            ctx->alt_bodies = in_block;
             seq_step(ctx, &t, in_block && pos > 0, in_block && pos < k - 1);
         }
+        ctx->alt_bodies = false;
         set_body_buffers(ctx, 1, 0);
         if ((st = check_launch(ctx)) != MG_OK) return st;
         MG_CK(cudaStreamSynchronize(ctx->stream));
@@ -1363,6 +1383,7 @@ static mg_status step_host_pipelined(mg_context *ctx, mg_atom_element *atoms, mg
             if ((st = flush(z_done, z_to)) != MG_OK) return st;
             z_done = std::max(z_done, z_to);
         }
+        if (mx) launch_skin_advance(lc, ctx->s);  // after the last density slab (no firststep since)
         launch_ghost_df_planes(lc, g, ctx->s, ctx->in, mx, -1, -1);
         launch_lat_force_sites(lc, g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, true, mx, u[SS - 1], u[SS], true);
         if ((st = flush(z_done, g.Sz)) != MG_OK) return st;
@@ -1387,6 +1408,26 @@ mg_status mg_set_step_fusion(mg_context *ctx, int32_t steps_per_graph) {
     if (!ctx || steps_per_graph < 0 || steps_per_graph > 256) return MG_ERR_ARG;
     ctx->fuse_steps = steps_per_graph;
     if (ctx->graph_multi) { cudaGraphExecDestroy(ctx->graph_multi); ctx->graph_multi = nullptr; }
+    return MG_OK;
+}
+
+mg_status mg_set_neighbour_skin(mg_context *ctx, double skin) {
+    if (!ctx || !(skin >= 0.0) || skin > ctx->g.a0) return MG_ERR_ARG;
+    set_skin(ctx->g, skin);
+    launch_skin_dirty(ctx->lc(), ctx->s);
+    ctx->graph_stale = true;  // the captured kernels hold the old geometry
+    ctx->gen++;
+    if (ctx->graph_multi) { cudaGraphExecDestroy(ctx->graph_multi); ctx->graph_multi = nullptr; }
+    return check_launch(ctx);
+}
+
+mg_status mg_skin_stats(mg_context *ctx, int64_t *passes, int64_t *rebuilds) {
+    if (!ctx || !passes || !rebuilds) return MG_ERR_ARG;
+    SkinState k;
+    MG_CK(cudaMemcpyAsync(&k, ctx->s.skin, sizeof(k), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_CK(cudaStreamSynchronize(ctx->stream));
+    *passes = static_cast<int64_t>(k.passes);
+    *rebuilds = static_cast<int64_t>(k.rebuilds);
     return MG_OK;
 }
 

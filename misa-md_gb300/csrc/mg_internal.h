@@ -16,10 +16,11 @@ constexpr double kBoltz = 8.617343e-5;       // src/types/pre_define.h:11
 constexpr double kMvv2e = 1.0364269e-4;      // src/types/pre_define.h:18
 constexpr double kFtm2v = (1.0 / kMvv2e);    // src/types/pre_define.h:19
 constexpr double kNeiLatCutoff = 0.5;        // src/md_building_config.h.in:24
-constexpr int kMaxFull = 232;
+constexpr int kMaxFull = 232;                // capacity of a full offset table per parity
 constexpr int kFirstThreads = 256;           // firststep block = one group of displaced flags (8 per lane)
-constexpr int kSortSmemKeys = 16384;
-constexpr int kVoteWords = 4;                // vote bits per 32-site group: pruned candidates up to 128         // bucket keys the list manager sorts in shared memory                // capacity of a full offset table per parity
+constexpr int kSortSmemKeys = 16384;         // bucket keys the list manager sorts in shared memory
+constexpr int kVoteWords = 4;                // vote bits per 32-site group: pruned candidates up to 128
+constexpr int kSkinSlots = 64;               // words the per-step maximum displacement is spread over
 
 // box flags (src/lattice/box.h:12-20)
 constexpr uint32_t kInBox = 0, kXLow = 1u, kXHigh = 2u, kYLow = 4u, kYHigh = 8u, kZLow = 16u, kZHigh = 32u;
@@ -66,10 +67,28 @@ struct Geom {
     float h_f;               // a0 / 2 (float)
     float rc2_h;             // (rc / h)^2 in half-lattice units
     float rc2_pre;           // rc2_h * (1 + 1e-4): FP32 candidate test of the FP64 gathers
+    float skin_h;            // Verlet skin of the near words, half-lattice units (0: off)
+    float rcs2_h;            // ((rc + skin) / h)^2 (rc2_h when the skin is off)
     // site_half[m] = RN((m / 2) a0), m in [0, n_site_half): the coordinate of half-lattice index m,
     // rounded as the site formula of decide rounds it (x: m = i; y, z: m = 2j + parity)
     const double *site_half;
     int n_site_half;
+};
+
+// Verlet skin on the group candidate lists (mixed form). The density pass of some step built the
+// near words from the displacement records of that step. Until `dirty` is set, no record has changed
+// since then except through firststep, and every change of a record is at most the maximum change
+// of its step (the step_max2 words); acc sums those maxima since the build. A pair inside rc now
+// was therefore inside rc + 2 acc when the words were built, and while 2 acc stays below the skin the
+// near words hold every pair inside the cutoff.
+struct SkinState {
+    unsigned step_max2[kSkinSlots];  // this step's max |du|^2 (float bits, half-lattice units)
+    float acc;                       // the sum of the per-step maxima of |du| since the build
+    int dirty;                       // a record changed outside firststep: the next pass rebuilds
+    int rebuilt;                     // the last density pass rebuilt the near words
+    int pad;
+    unsigned long long rebuilds;     // density passes that rebuilt the near words
+    unsigned long long passes;       // density passes with near words
 };
 
 // Lattice slot arrays (structure of arrays over every slot, ghosts included).
@@ -85,6 +104,8 @@ struct Slots {
     float4 *u4;              // displacement from the site in half-lattice units, w = type bits
     float4 *u4n;             // the next loop body's u4 buffer when the force pass takes the next firststep
     unsigned *umask;         // per 32-site group and parity: kVoteWords words of votes on the pruned candidates
+    unsigned *near;          // the same groups: the pruned candidates inside rc + skin when last built
+    SkinState *skin;
     float *df32;             // F'(rho) in float
 };
 
@@ -226,8 +247,10 @@ enum { PACK_ALL = 0xff, PACK_RHO = 1, PACK_DF = 2, PACK_F = 4 };
 
 // local atoms [t0, t1) in k, j, i order (t1 < 0: all)
 // fused: the previous force pass took this firststep already (launch_lat_force with fuse_next)
+// alt: a body of a graph whose bodies alternate their u4 buffers (the previous body's records are in
+// s.u4n)
 void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const StepParams *sp, bool decide, int t0 = 0,
-                      int t1 = -1, bool fused = false);
+                      int t1 = -1, bool fused = false, bool alt = false);
 // fill g.site_half (once per context)
 void launch_site_table(const LaunchCtx &lc, const Geom &g, double *site_half);
 void launch_decide_scan(const LaunchCtx &lc, const Geom &g, Slots s, Inter in);
@@ -246,6 +269,11 @@ void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTa
 void launch_lat_rho_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, int u0, int u1,
                           bool votes = false);
 bool votes_ok(const LaunchCtx &lc, const Geom &g);
+// after the density pass of a step that used the near words, before the next firststep: fold the
+// step's maximum displacement into the skin's sum (or restart it when the pass rebuilt the words)
+void launch_skin_advance(const LaunchCtx &lc, Slots s);
+// a displacement record changed outside firststep: the next density pass rebuilds the near words
+void launch_skin_dirty(const LaunchCtx &lc, Slots s);
 // forward df for the ghost slots inside local planes [k0, k1), or (k0 < 0) the ghost planes below and
 // above the box plus the ghost inter atoms
 void launch_ghost_df_planes(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool mixed, int k0, int k1);

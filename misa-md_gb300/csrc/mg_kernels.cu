@@ -328,6 +328,7 @@ void launch_unpack_aos(const LaunchCtx &lc, const Geom &g, const mg_atom_element
     if (s1 <= s0) return;
     const int b = 256;
     k_unpack_aos<<<(s1 - s0 + b - 1) / b, b, 0, lc.stream>>>(g, aos, s, in, types_ok_mask, mixed, s0, s1);
+    launch_skin_dirty(lc, s);
 }
 __global__ void k_set_counts(Inter in, int n_inter) {
     in.cnt[CNT_INTER] = n_inter;
@@ -373,14 +374,24 @@ __device__ __noinline__ bool exact_displaced(double ex, double ey, double ez, do
     return d;
 }
 
+// the step's largest change of a displacement record: one reduction per group of converged lanes and
+// one atomic max per group, spread over kSkinSlots words (squares of non-negative floats order like
+// their bit patterns; a NaN orders above every number, so it forces a rebuild)
+__device__ __forceinline__ void skin_note(const Slots &s, float d2) {
+    const unsigned m = __activemask();
+    const unsigned v = __reduce_max_sync(m, __float_as_uint(d2));
+    if ((int) (threadIdx.x & 31) == __ffs(m) - 1) atomicMax(&s.skin->step_max2[blockIdx.x & (kSkinSlots - 1)], v);
+}
+
 // NewtonMotion::firststep for one lattice atom (src/newton_motion.cpp:30-55) and decide's displacement
 // test (src/atom.cpp:34-42): v += c f, x += dt v (each operation rounded as the reference rounds it),
 // the displacement record u4 (written to u4_out, parity-split index) and the displaced flag of local
-// index t. MOVE = false: the test alone, on the current positions.
+// index t. MOVE = false: the test alone, on the current positions. u4_prev holds the record the last
+// density pass read (for the skin's displacement bound).
 template <bool MOVE, bool DECIDE>
 __device__ __forceinline__ void first_half(const Geom &g, const Slots &s, const Inter &in, const StepParams *__restrict__ p,
                                            int sl, int t, int i, int j, int k, int ty, double vx, double vy, double vz,
-                                           double fx, double fy, double fz, float4 *u4_out) {
+                                           double fx, double fy, double fz, float4 *u4_out, const float4 *u4_prev) {
     double x = s.x[sl], y = s.y[sl], z = s.z[sl];
     if (MOVE) {
         const double c = dt_inv_m_of(p, ty);
@@ -402,7 +413,14 @@ __device__ __forceinline__ void first_half(const Geom &g, const Slots &s, const 
     const float exf = __double2float_rn(ex), eyf = __double2float_rn(ey), ezf = __double2float_rn(ez);
     if (MOVE) {
         const float ih = g.inv_h_f;
-        u4_out[sidx(g, sl)] = make_float4(exf * ih, eyf * ih, ezf * ih, __int_as_float(ty));
+        const float4 nu = make_float4(exf * ih, eyf * ih, ezf * ih, __int_as_float(ty));
+        const int si = sidx(g, sl);
+        if (g.skin_h > 0.f) {  // read before the store: in place, u4_prev is u4_out
+            const float4 o = u4_prev[si];
+            const float dx = nu.x - o.x, dy = nu.y - o.y, dz = nu.z - o.z;
+            skin_note(s, dx * dx + dy * dy + dz * dz);
+        }
+        u4_out[si] = nu;
     }
     if (DECIDE) {
         // the exact FP64 test of decide runs only where the FP32 distance is not clearly below it
@@ -417,9 +435,11 @@ __device__ __forceinline__ void first_half(const Geom &g, const Slots &s, const 
 // its displacement records into this step's u4 buffer (when no inter atoms exist; else the work is
 // done here). Every local slot's u4 is written, vacancies included, so the two buffers a fused graph
 // alternates between are always complete.
+// alt: inside a graph whose bodies alternate their u4 buffers, where the previous body's records are
+// in s.u4n
 template <bool MOVE, bool DECIDE>
 __global__ void __launch_bounds__(kFirstThreads) k_firststep(Geom g, Slots s, Inter in, const StepParams *__restrict__ p,
-                                                             int t0, int t1, bool fused) {
+                                                             int t0, int t1, bool fused, bool alt) {
     const int t = t0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= t1) return;
     if (fused && lattice_only(in)) return;
@@ -433,9 +453,9 @@ __global__ void __launch_bounds__(kFirstThreads) k_firststep(Geom g, Slots s, In
     }
     if (MOVE)
         first_half<true, DECIDE>(g, s, in, p, sl, t, i, j, k, ty, s.vx[sl], s.vy[sl], s.vz[sl], s.fx[sl], s.fy[sl],
-                                 s.fz[sl], s.u4);
+                                 s.fz[sl], s.u4, alt ? s.u4n : s.u4);
     else
-        first_half<false, DECIDE>(g, s, in, p, sl, t, i, j, k, ty, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, s.u4);
+        first_half<false, DECIDE>(g, s, in, p, sl, t, i, j, k, ty, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, s.u4, s.u4);
 }
 
 // one warp per group of kFirstThreads flag bytes (8 per lane, read as one 64-bit word): its count
@@ -524,16 +544,16 @@ __global__ void k_disp_collect(Geom g, Inter in, int nblocks) {
 }
 
 void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, const StepParams *p, bool decide, int t0,
-                      int t1, bool fused) {
+                      int t1, bool fused, bool alt) {
     if (t1 < 0) t1 = g.n_local;
     if (t1 <= t0) return;
     const int b = kFirstThreads, n = (t1 - t0 + b - 1) / b;
-    if (decide) k_firststep<true, true><<<n, b, 0, lc.stream>>>(g, s, in, p, t0, t1, fused);
-    else k_firststep<true, false><<<n, b, 0, lc.stream>>>(g, s, in, p, t0, t1, fused);
+    if (decide) k_firststep<true, true><<<n, b, 0, lc.stream>>>(g, s, in, p, t0, t1, fused, alt);
+    else k_firststep<true, false><<<n, b, 0, lc.stream>>>(g, s, in, p, t0, t1, fused, alt);
 }
 void launch_decide_scan(const LaunchCtx &lc, const Geom &g, Slots s, Inter in) {
     const int b = kFirstThreads, n = (g.n_local + b - 1) / b;
-    k_firststep<false, true><<<n, b, 0, lc.stream>>>(g, s, in, nullptr, 0, g.n_local, false);
+    k_firststep<false, true><<<n, b, 0, lc.stream>>>(g, s, in, nullptr, 0, g.n_local, false, false);
 }
 void launch_displaced_collect(const LaunchCtx &lc, const Geom &g, Inter in) {
     const int nblocks = (g.n_local + kFirstThreads - 1) / kFirstThreads;
@@ -788,14 +808,39 @@ __device__ __forceinline__ void rho_sum_mixed(const NeighTables &nt, const Geom 
 // the pruned candidates [q0, q1), q1 - q0 <= 32, noting which this site has inside the cutoff (bit j:
 // candidate q0 + j). The bit is set inside the in-range branch, so the notes cost next to nothing.
 // FULL: q1 - q0 is 32, known at compile time (the full chunks; a runtime count there costs registers).
+// Also notes, in nb, the candidates inside rc + skin (rcs2_h >= rc2_h).
 template <int PAR, bool FULL>
 __device__ __forceinline__ unsigned rho_sum_noted(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt,
-                                                  int si, float4 ui, int q0, int q1, float &sum, float &comp) {
+                                                  int si, float4 ui, int q0, int q1, float &sum, float &comp, unsigned &nb) {
     const float rc2 = g.rc2_h;
     const f2 uixy = f2_pack(ui.x, ui.y);
     unsigned bits = 0;
 #pragma unroll 2
     for (int j = 0; j < (FULL ? 32 : q1 - q0); j++) {
+        const float4 D = nt.cand[PAR][q0 + j];
+        const float4 uj = __ldg(s.u4 + si + __float_as_int(D.w));
+        f2 dxy; float dz;
+        const float r2 = pair_r2(uixy, ui.z, D, uj, dxy, dz);
+        if (r2 < g.rcs2_h) {
+            nb |= 1u << j;
+            if (r2 < rc2) {
+                rho_pair(pt, r2, uj, sum, comp);
+                bits |= 1u << j;
+            }
+        }
+    }
+    return bits;
+}
+// the candidates q0 + j of the set bits j of `word` (the group's near words), in increasing order, so
+// the in-range pairs are summed in the same order as by the full loop
+template <int PAR>
+__device__ __forceinline__ unsigned rho_sum_near(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt,
+                                                 int si, float4 ui, int q0, unsigned word, float &sum, float &comp) {
+    const float rc2 = g.rc2_h;
+    const f2 uixy = f2_pack(ui.x, ui.y);
+    unsigned bits = 0;
+    for (unsigned w = word; w; w &= w - 1) {
+        const int j = __ffs(w) - 1;
         const float4 D = nt.cand[PAR][q0 + j];
         const float4 uj = __ldg(s.u4 + si + __float_as_int(D.w));
         f2 dxy; float dz;
@@ -807,35 +852,65 @@ __device__ __forceinline__ unsigned rho_sum_noted(const NeighTables &nt, const G
     }
     return bits;
 }
+// Whether this density pass rebuilds the near words: the same answer in every thread of the grid, as
+// nothing it reads changes during the pass (all 32 lanes of the warp call it). The margin covers the
+// FP32 rounding of the distances and of the sums, which is below 1e-5 half-lattice units.
+constexpr float kSkinMargin = 1e-3f;
+__device__ __forceinline__ bool skin_full(const Geom &g, const Slots &s) {
+    if (!(g.skin_h > 0.f)) return true;
+    const SkinState *k = s.skin;
+    const int lane = threadIdx.x & 31;
+    const unsigned m = __reduce_max_sync(0xffffffffu, max(k->step_max2[lane], k->step_max2[lane + 32]));
+    const float step = sqrtf(__uint_as_float(m));
+    return k->dirty != 0 || !(2.f * (k->acc + step) + kSkinMargin <= g.skin_h);
+}
 __device__ __forceinline__ unsigned *group_words(const Geom &g, const Slots &s, int par, int u) {
     return s.umask + kVoteWords * (par * ((g.n_local_half + 31) >> 5) + (u >> 5));
 }
 
-// votes: write the group words of the pruned tail (all 32 lanes of the warp call this, with valid
-// false for threads past the end; the warp covers one 32-site group of one parity)
+// votes: write the group's vote words (all 32 lanes of the warp call this, with valid false for
+// threads past the end; the warp covers one 32-site group of one parity). full: visit every pruned
+// candidate and rebuild the group's near words; else visit the near words' candidates only.
 __device__ __forceinline__ void k_lat_rho_mixed_site(int t, bool valid, const NeighTables &nt, const Geom &g, const Slots &s, const Inter &in,
-                                                     const PotTables &pt, bool hook, int order, bool votes) {
+                                                     const PotTables &pt, bool hook, int order, bool votes, bool full) {
     int par = 0, u = 0;
     const int sl = valid ? gather_site(g, t, order, par, u) : -1;
     const int si = sl >= 0 ? sidx(g, sl) : 0;
     const float4 ui = sl >= 0 ? s.u4[si] : vacant_u4();
     const int ti = __float_as_int(ui.w);
     const unsigned live = votes ? __ballot_sync(0xffffffffu, ti >= 0) : 0u;
+    // a site marked by a far or just recombined atom nearby makes its group rebuild its lists: that
+    // atom's record did not come from firststep, so the skin's bound does not cover it
+    if (votes && !full) full = __any_sync(0xffffffffu, sl >= 0 && in.far_flag[sl]);
     if (sl < 0) return;
     if (ti < 0) { s.rho[sl] = 0.0; return; }
     float sum = 0.f, comp = 0.f;
     const int np = nt.npruned;
     if (votes) {  // 32 candidates per vote word; the group's word: any live site of the warp
         unsigned *w = group_words(g, s, par, u);
+        unsigned *nw = s.near + (w - s.umask);
         const bool leader = (int) (threadIdx.x & 31) == __ffs(live) - 1;
-        for (int k = 0; k * 32 < np; k++) {
-            const int q0 = 32 * k, q1 = min(q0 + 32, np);
-            const unsigned bits = q1 - q0 == 32 ? (par ? rho_sum_noted<1, true>(nt, g, s, pt, si, ui, q0, q1, sum, comp)
-                                                       : rho_sum_noted<0, true>(nt, g, s, pt, si, ui, q0, q1, sum, comp))
-                                                : (par ? rho_sum_noted<1, false>(nt, g, s, pt, si, ui, q0, q1, sum, comp)
-                                                       : rho_sum_noted<0, false>(nt, g, s, pt, si, ui, q0, q1, sum, comp));
-            const unsigned any = __reduce_or_sync(live, bits);
-            if (leader) w[k] = any;
+        if (full) {
+            for (int k = 0; k * 32 < np; k++) {
+                const int q0 = 32 * k, q1 = min(q0 + 32, np);
+                unsigned nb = 0;
+                const unsigned bits = q1 - q0 == 32 ? (par ? rho_sum_noted<1, true>(nt, g, s, pt, si, ui, q0, q1, sum, comp, nb)
+                                                           : rho_sum_noted<0, true>(nt, g, s, pt, si, ui, q0, q1, sum, comp, nb))
+                                                    : (par ? rho_sum_noted<1, false>(nt, g, s, pt, si, ui, q0, q1, sum, comp, nb)
+                                                           : rho_sum_noted<0, false>(nt, g, s, pt, si, ui, q0, q1, sum, comp, nb));
+                const unsigned any = __reduce_or_sync(live, bits);
+                const unsigned anyn = __reduce_or_sync(live, nb);
+                if (leader) { w[k] = any; nw[k] = anyn; }
+            }
+        } else {
+            const uint4 n4 = *reinterpret_cast<const uint4 *>(nw);
+            for (int k = 0; k * 32 < np; k++) {
+                const unsigned word = k == 0 ? n4.x : k == 1 ? n4.y : k == 2 ? n4.z : n4.w;
+                const unsigned bits = par ? rho_sum_near<1>(nt, g, s, pt, si, ui, 32 * k, word, sum, comp)
+                                          : rho_sum_near<0>(nt, g, s, pt, si, ui, 32 * k, word, sum, comp);
+                const unsigned any = __reduce_or_sync(live, bits);
+                if (leader) w[k] = any;
+            }
         }
     } else {
         if (par) rho_sum_mixed<1>(nt, g, s, pt, si, ui, 0, np, sum, comp);
@@ -859,11 +934,13 @@ __global__ void __launch_bounds__(512, 4) k_lat_rho_mixed(const __grid_constant_
                                                        int nthreads, bool votes) {
     const int t0 = tbase + blockIdx.x * blockDim.x + threadIdx.x;  // threads [tbase, nthreads)
     if (!LOOP) {
-        k_lat_rho_mixed_site(t0, t0 < nthreads, nt, g, s, in, pt, hook, order, votes);
+        const bool full = votes && skin_full(g, s);
+        if (full && blockIdx.x == 0 && threadIdx.x == 0) s.skin->rebuilt = 1;
+        k_lat_rho_mixed_site(t0, t0 < nthreads, nt, g, s, in, pt, hook, order, votes, full);
         return;
     }
     for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x)
-        k_lat_rho_mixed_site(t, true, nt, g, s, in, pt, hook, order, false);
+        k_lat_rho_mixed_site(t, true, nt, g, s, in, pt, hook, order, false, true);
 }
 
 // atoms per thread: each thread takes rho_apt sites, one grid stride apart (the stride is a multiple
@@ -889,9 +966,37 @@ static void launch_lat_rho_threads(const LaunchCtx &lc, const Geom &g, Slots s, 
         else k_lat_rho_fp64<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, tb, te);
     }
 }
+// one block of kSkinSlots threads
+__global__ void __launch_bounds__(kSkinSlots) k_skin_advance(SkinState *k) {
+    __shared__ unsigned wmax[kSkinSlots / 32];
+    unsigned v = k->step_max2[threadIdx.x];
+    k->step_max2[threadIdx.x] = 0u;
+    v = __reduce_max_sync(0xffffffffu, v);
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    unsigned m = 0u;
+    for (int w = 0; w < kSkinSlots / 32; w++) m = max(m, wmax[w]);
+    if (k->rebuilt) {  // built on this step's records: the sum restarts
+        k->acc = 0.f;
+        k->dirty = 0;
+        k->rebuilt = 0;
+        k->rebuilds++;
+    } else {
+        k->acc += sqrtf(__uint_as_float(m));  // a NaN or infinity forces the next pass to rebuild
+    }
+    k->passes++;
+}
+void launch_skin_advance(const LaunchCtx &lc, Slots s) { k_skin_advance<<<1, kSkinSlots, 0, lc.stream>>>(s.skin); }
+void launch_skin_dirty(const LaunchCtx &lc, Slots s) { cudaMemsetAsync(&s.skin->dirty, 1, 1, lc.stream); }
+
+// A voted mixed pass is followed by the skin's advance. A mixed pass without votes leaves the near
+// words behind the positions, so the next voted pass rebuilds them.
 void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook, bool votes) {
-    launch_lat_rho_threads(lc, g, s, in, t, mixed, hook, 0, gather_threads(g, lc.rho_order),
-                           votes && mixed && !hook && votes_ok(lc, g));
+    const bool v = votes && mixed && !hook && votes_ok(lc, g);
+    launch_lat_rho_threads(lc, g, s, in, t, mixed, hook, 0, gather_threads(g, lc.rho_order), v);
+    if (v) launch_skin_advance(lc, s);
+    else if (mixed) launch_skin_dirty(lc, s);
 }
 // thread range of the sites [u0, u1) of both parities (u0, u1 multiples of 32, or u1 = n_local_half)
 static void site_threads(const Geom &g, int order, int u0, int u1, int tb[2], int te[2], int &nr) {
@@ -912,6 +1017,7 @@ void launch_lat_rho_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in,
     site_threads(g, lc.rho_order, u0, u1, tb, te, nr);
     const bool v = votes && mixed && votes_ok(lc, g);
     for (int r = 0; r < nr; r++) launch_lat_rho_threads(lc, g, s, in, t, mixed, false, tb[r], te[r], v);
+    if (!v && mixed) launch_skin_dirty(lc, s);  // the caller advances the skin after the last slab
 }
 
 // dF/drho when inter atoms added density after the lattice pass (or for the df hook)
@@ -1151,7 +1257,7 @@ __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables 
             // body's buffer, u4n)
             int i, j, k;
             const int tl = local_index_of(g, sl, i, j, k);
-            first_half<true, true>(g, s, in, sp, sl, tl, i, j, k, ti, vx, vy, vz, fx, fy, fz, s.u4n);
+            first_half<true, true>(g, s, in, sp, sl, tl, i, j, k, ti, vx, vy, vz, fx, fy, fz, s.u4n, s.u4);
         }
     }
 }
@@ -1583,8 +1689,12 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
                 site_of(g, X, Y, Z, xs, ys, zs);
                 s.u4[sidx(g, sl)] = make_u4(g, in.x[a], in.y[a], in.z[a], xs, ys, zs, in.type[a]);
             }
-            // a recombined atom may sit up to sqrt(5)/4 a0 from its new site
-            if (displaced_fp64(g, s, sl)) {
+            // A recombined atom may sit up to sqrt(5)/4 a0 from its new site. Every recombined atom
+            // joins this step's far list: the marks on its neighbourhood also make the density pass
+            // rebuild the candidate lists of the groups that can see it (its record did not come
+            // from firststep). The tail pairs the marks add for an atom within 0.2 a0 of its site
+            // are all beyond the cutoff, so they change no sum.
+            {
                 const int q = atomicAdd(&in.cnt[CNT_FAR], 1);
                 if (q < in.fcap) in.far_list[q] = sl;
                 else set_error(in, MG_DEVERR_DISPLACED_OVERFLOW);
