@@ -200,8 +200,8 @@ void seq_eam_lists(mg_context *ctx, bool with_manage_prefix, int manage_mask, Ti
     launch_ghost_copy(lc, ctx->g, ctx->s, mx);
     if (t) t->mark(4);
 }
-// rho, dF/drho and the forward df exchange; the density pass leaves the tail votes for the force pass
-// that follows it on the same positions
+// rho, dF/drho and the forward df exchange; the density pass checks or rebuilds the group lists that
+// the force pass on the same positions walks
 void seq_eam_rho(mg_context *ctx, Timer *t) {
     const LaunchCtx lc = ctx->lc();
     const bool mx = ctx->mixed();
@@ -549,8 +549,7 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     ALLOC(s.rho, ns); ALLOC(s.df, ns); ALLOC(s.e, ns);
     ALLOC(s.type, ns); ALLOC(s.id, ns);
     ALLOC(s.u4, ns); ALLOC(s.u4n, ns); ALLOC(s.df32, ns);
-    ALLOC(s.umask, static_cast<size_t>(2 * kVoteWords * ((g.n_local_half + 31) / 32)));
-    ALLOC(s.near, static_cast<size_t>(2 * kVoteWords * ((g.n_local_half + 31) / 32)));
+    ALLOC(s.near, static_cast<size_t>(2 * kListWords * ((g.n_local_half + 31) / 32)));
     ALLOC(s.skin, 1);
     ctx->u4_main = s.u4;
     ctx->u4_alt = s.u4n;

@@ -19,7 +19,7 @@ constexpr double kNeiLatCutoff = 0.5;        // src/md_building_config.h.in:24
 constexpr int kMaxFull = 232;                // capacity of a full offset table per parity
 constexpr int kFirstThreads = 256;           // firststep block = one group of displaced flags (8 per lane)
 constexpr int kSortSmemKeys = 16384;         // bucket keys the list manager sorts in shared memory
-constexpr int kVoteWords = 4;                // vote bits per 32-site group: pruned candidates up to 128
+constexpr int kListWords = 4;                // list bits per 32-site group: pruned candidates up to 128
 constexpr int kSkinSlots = 64;               // words the per-step maximum displacement is spread over
 
 // box flags (src/lattice/box.h:12-20)
@@ -103,8 +103,8 @@ struct Slots {
     // mixed form, parity-split layout (slot s at (s & 1) * half + (s >> 1)):
     float4 *u4;              // displacement from the site in half-lattice units, w = type bits
     float4 *u4n;             // the next loop body's u4 buffer when the force pass takes the next firststep
-    unsigned *umask;         // per 32-site group and parity: kVoteWords words of votes on the pruned candidates
-    unsigned *near;          // the same groups: the pruned candidates inside rc + skin when last built
+    unsigned *near;          // per 32-site group and parity: kListWords words, the pruned candidates some
+                             // site of the group had inside rc + skin when the list was last built
     SkinState *skin;
     float *df32;             // F'(rho) in float
 };
@@ -261,14 +261,15 @@ void launch_far_clear(const LaunchCtx &lc, const Geom &g, Inter in);
 void launch_far_mark(const LaunchCtx &lc, const Geom &g, Inter in);
 void launch_ghost_copy(const LaunchCtx &lc, const Geom &g, Slots s, bool mixed);
 void launch_ghost_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool mixed);
-// votes (mixed form): leave, per 32-site group, which pruned candidates any site has inside the
-// cutoff, for the force pass of the same step (when votes_ok; the force pass must get the same flag)
+// lists (mixed form): check or rebuild, per 32-site group, the list of pruned candidates that some site
+// of the group has inside rc + skin, and visit only those (when lists_ok; the force pass of the same
+// step must get the same flag)
 void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook,
-                    bool votes = false);
+                    bool lists = false);
 // the density pass over the sites [u0, u1) of both parities (as launch_lat_force_sites)
 void launch_lat_rho_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, int u0, int u1,
-                          bool votes = false);
-bool votes_ok(const LaunchCtx &lc, const Geom &g);
+                          bool lists = false);
+bool lists_ok(const LaunchCtx &lc, const Geom &g);
 // after the density pass of a step that used the near words, before the next firststep: fold the
 // step's maximum displacement into the skin's sum (or restart it when the pass rebuilt the words)
 void launch_skin_advance(const LaunchCtx &lc, Slots s);
@@ -281,11 +282,11 @@ void launch_lat_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTab
 // fuse_next (mixed form, kick, fixed dt): after the second half-kick each lattice atom also takes the
 // next step's firststep (into u4n), when no inter atoms exist
 void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *sp, bool kick,
-                      bool mixed, bool hook, bool fuse_next = false, bool votes = false);
+                      bool mixed, bool hook, bool fuse_next = false, bool lists = false);
 // the force pass over the sites of both parities whose index within their parity is in [u0, u1):
 // with u0 and u1 multiples of 32 (or u1 = n_local_half) the slabs of a split pass are disjoint warps
 void launch_lat_force_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *sp, bool kick,
-                            bool mixed, int u0, int u1, bool votes = false);
+                            bool mixed, int u0, int u1, bool lists = false);
 void launch_secondstep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams *sp, bool lattice);
 // step head: records the step's dt and, in variable mode, sets dt from the last kick's max |v|
 void launch_step_head(const LaunchCtx &lc, StepParams *sp);

@@ -805,16 +805,15 @@ __device__ __forceinline__ void rho_sum_mixed(const NeighTables &nt, const Geom 
         if (r2 < rc2) rho_pair(pt, r2, uj, sum, comp);  // false for vacancies (NaN coordinates)
     }
 }
-// the pruned candidates [q0, q1), q1 - q0 <= 32, noting which this site has inside the cutoff (bit j:
-// candidate q0 + j). The bit is set inside the in-range branch, so the notes cost next to nothing.
-// FULL: q1 - q0 is 32, known at compile time (the full chunks; a runtime count there costs registers).
-// Also notes, in nb, the candidates inside rc + skin (rcs2_h >= rc2_h).
+// The pruned candidates [q0, q1), q1 - q0 <= 32, noting which this site has within rc + skin (bit j:
+// candidate q0 + j; rcs2_h >= rc2_h). FULL: q1 - q0 is 32, known at compile time (the full chunks; a
+// runtime count there costs registers).
 template <int PAR, bool FULL>
 __device__ __forceinline__ unsigned rho_sum_noted(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt,
-                                                  int si, float4 ui, int q0, int q1, float &sum, float &comp, unsigned &nb) {
+                                                  int si, float4 ui, int q0, int q1, float &sum, float &comp) {
     const float rc2 = g.rc2_h;
     const f2 uixy = f2_pack(ui.x, ui.y);
-    unsigned bits = 0;
+    unsigned nb = 0;
 #pragma unroll 2
     for (int j = 0; j < (FULL ? 32 : q1 - q0); j++) {
         const float4 D = nt.cand[PAR][q0 + j];
@@ -823,36 +822,28 @@ __device__ __forceinline__ unsigned rho_sum_noted(const NeighTables &nt, const G
         const float r2 = pair_r2(uixy, ui.z, D, uj, dxy, dz);
         if (r2 < g.rcs2_h) {
             nb |= 1u << j;
-            if (r2 < rc2) {
-                rho_pair(pt, r2, uj, sum, comp);
-                bits |= 1u << j;
-            }
+            if (r2 < rc2) rho_pair(pt, r2, uj, sum, comp);
         }
     }
-    return bits;
+    return nb;
 }
-// the candidates q0 + j of the set bits j of `word` (the group's near words), in increasing order, so
-// the in-range pairs are summed in the same order as by the full loop
+// the candidates q0 + j of the set bits j of `word` (a word of the group's list), in increasing order,
+// so the in-range pairs are summed in the same order as by the full loop
 template <int PAR>
-__device__ __forceinline__ unsigned rho_sum_near(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt,
-                                                 int si, float4 ui, int q0, unsigned word, float &sum, float &comp) {
+__device__ __forceinline__ void rho_sum_listed(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt,
+                                               int si, float4 ui, int q0, unsigned word, float &sum, float &comp) {
     const float rc2 = g.rc2_h;
     const f2 uixy = f2_pack(ui.x, ui.y);
-    unsigned bits = 0;
     for (unsigned w = word; w; w &= w - 1) {
         const int j = __ffs(w) - 1;
         const float4 D = nt.cand[PAR][q0 + j];
         const float4 uj = __ldg(s.u4 + si + __float_as_int(D.w));
         f2 dxy; float dz;
         const float r2 = pair_r2(uixy, ui.z, D, uj, dxy, dz);
-        if (r2 < rc2) {
-            rho_pair(pt, r2, uj, sum, comp);
-            bits |= 1u << j;
-        }
+        if (r2 < rc2) rho_pair(pt, r2, uj, sum, comp);
     }
-    return bits;
 }
-// Whether this density pass rebuilds the near words: the same answer in every thread of the grid, as
+// Whether this density pass rebuilds the group lists: the same answer in every thread of the grid, as
 // nothing it reads changes during the pass (all 32 lanes of the warp call it). The margin covers the
 // FP32 rounding of the distances and of the sums, which is below 1e-5 half-lattice units.
 constexpr float kSkinMargin = 1e-3f;
@@ -864,52 +855,48 @@ __device__ __forceinline__ bool skin_full(const Geom &g, const Slots &s) {
     const float step = sqrtf(__uint_as_float(m));
     return k->dirty != 0 || !(2.f * (k->acc + step) + kSkinMargin <= g.skin_h);
 }
-__device__ __forceinline__ unsigned *group_words(const Geom &g, const Slots &s, int par, int u) {
-    return s.umask + kVoteWords * (par * ((g.n_local_half + 31) >> 5) + (u >> 5));
+// the list of the 32-site group of parity par holding site u: kListWords words over the pruned candidates
+__device__ __forceinline__ unsigned *group_list(const Geom &g, const Slots &s, int par, int u) {
+    return s.near + kListWords * (par * ((g.n_local_half + 31) >> 5) + (u >> 5));
 }
 
-// votes: write the group's vote words (all 32 lanes of the warp call this, with valid false for
-// threads past the end; the warp covers one 32-site group of one parity). full: visit every pruned
-// candidate and rebuild the group's near words; else visit the near words' candidates only.
+// lists: use the group lists (all 32 lanes of the warp call this, with valid false for threads past
+// the end; the warp covers one 32-site group of one parity). full: visit every pruned candidate and
+// rebuild the group's list; else visit the listed candidates only.
 __device__ __forceinline__ void k_lat_rho_mixed_site(int t, bool valid, const NeighTables &nt, const Geom &g, const Slots &s, const Inter &in,
-                                                     const PotTables &pt, bool hook, int order, bool votes, bool full) {
+                                                     const PotTables &pt, bool hook, int order, bool lists, bool full) {
     int par = 0, u = 0;
     const int sl = valid ? gather_site(g, t, order, par, u) : -1;
     const int si = sl >= 0 ? sidx(g, sl) : 0;
     const float4 ui = sl >= 0 ? s.u4[si] : vacant_u4();
     const int ti = __float_as_int(ui.w);
-    const unsigned live = votes ? __ballot_sync(0xffffffffu, ti >= 0) : 0u;
-    // a site marked by a far or just recombined atom nearby makes its group rebuild its lists: that
+    const unsigned live = lists ? __ballot_sync(0xffffffffu, ti >= 0) : 0u;
+    // a site marked by a far or just recombined atom nearby makes its group rebuild its list: that
     // atom's record did not come from firststep, so the skin's bound does not cover it
-    if (votes && !full) full = __any_sync(0xffffffffu, sl >= 0 && in.far_flag[sl]);
+    if (lists && !full) full = __any_sync(0xffffffffu, sl >= 0 && in.far_flag[sl]);
     if (sl < 0) return;
     if (ti < 0) { s.rho[sl] = 0.0; return; }
     float sum = 0.f, comp = 0.f;
     const int np = nt.npruned;
-    if (votes) {  // 32 candidates per vote word; the group's word: any live site of the warp
-        unsigned *w = group_words(g, s, par, u);
-        unsigned *nw = s.near + (w - s.umask);
-        const bool leader = (int) (threadIdx.x & 31) == __ffs(live) - 1;
+    if (lists) {  // 32 candidates per list word; the group's word: any live site of the warp
+        unsigned *w = group_list(g, s, par, u);
         if (full) {
+            const bool leader = (int) (threadIdx.x & 31) == __ffs(live) - 1;
             for (int k = 0; k * 32 < np; k++) {
                 const int q0 = 32 * k, q1 = min(q0 + 32, np);
-                unsigned nb = 0;
-                const unsigned bits = q1 - q0 == 32 ? (par ? rho_sum_noted<1, true>(nt, g, s, pt, si, ui, q0, q1, sum, comp, nb)
-                                                           : rho_sum_noted<0, true>(nt, g, s, pt, si, ui, q0, q1, sum, comp, nb))
-                                                    : (par ? rho_sum_noted<1, false>(nt, g, s, pt, si, ui, q0, q1, sum, comp, nb)
-                                                           : rho_sum_noted<0, false>(nt, g, s, pt, si, ui, q0, q1, sum, comp, nb));
-                const unsigned any = __reduce_or_sync(live, bits);
-                const unsigned anyn = __reduce_or_sync(live, nb);
-                if (leader) { w[k] = any; nw[k] = anyn; }
+                const unsigned nb = q1 - q0 == 32 ? (par ? rho_sum_noted<1, true>(nt, g, s, pt, si, ui, q0, q1, sum, comp)
+                                                         : rho_sum_noted<0, true>(nt, g, s, pt, si, ui, q0, q1, sum, comp))
+                                                  : (par ? rho_sum_noted<1, false>(nt, g, s, pt, si, ui, q0, q1, sum, comp)
+                                                         : rho_sum_noted<0, false>(nt, g, s, pt, si, ui, q0, q1, sum, comp));
+                const unsigned any = __reduce_or_sync(live, nb);
+                if (leader) w[k] = any;
             }
         } else {
-            const uint4 n4 = *reinterpret_cast<const uint4 *>(nw);
+            const uint4 n4 = *reinterpret_cast<const uint4 *>(w);
             for (int k = 0; k * 32 < np; k++) {
                 const unsigned word = k == 0 ? n4.x : k == 1 ? n4.y : k == 2 ? n4.z : n4.w;
-                const unsigned bits = par ? rho_sum_near<1>(nt, g, s, pt, si, ui, 32 * k, word, sum, comp)
-                                          : rho_sum_near<0>(nt, g, s, pt, si, ui, 32 * k, word, sum, comp);
-                const unsigned any = __reduce_or_sync(live, bits);
-                if (leader) w[k] = any;
+                if (par) rho_sum_listed<1>(nt, g, s, pt, si, ui, 32 * k, word, sum, comp);
+                else rho_sum_listed<0>(nt, g, s, pt, si, ui, 32 * k, word, sum, comp);
             }
         }
     } else {
@@ -929,14 +916,14 @@ __device__ __forceinline__ void k_lat_rho_mixed_site(int t, bool valid, const Ne
         s.df32[si] = der_f(pt.F_dff + ti * pt.nrho, m, p);
     }
 }
-template <bool LOOP>  // LOOP: several sites per thread, one grid stride apart (no votes)
+template <bool LOOP>  // LOOP: several sites per thread, one grid stride apart (no group lists)
 __global__ void __launch_bounds__(512, 4) k_lat_rho_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool hook, int order, int tbase,
-                                                       int nthreads, bool votes) {
+                                                       int nthreads, bool lists) {
     const int t0 = tbase + blockIdx.x * blockDim.x + threadIdx.x;  // threads [tbase, nthreads)
     if (!LOOP) {
-        const bool full = votes && skin_full(g, s);
+        const bool full = lists && skin_full(g, s);
         if (full && blockIdx.x == 0 && threadIdx.x == 0) s.skin->rebuilt = 1;
-        k_lat_rho_mixed_site(t0, t0 < nthreads, nt, g, s, in, pt, hook, order, votes, full);
+        k_lat_rho_mixed_site(t0, t0 < nthreads, nt, g, s, in, pt, hook, order, lists, full);
         return;
     }
     for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x)
@@ -945,16 +932,16 @@ __global__ void __launch_bounds__(512, 4) k_lat_rho_mixed(const __grid_constant_
 
 // atoms per thread: each thread takes rho_apt sites, one grid stride apart (the stride is a multiple
 // of 64, so warps keep their parity and thread order)
-// The density pass can leave per-group votes on the pruned candidates for the force pass of the same
-// step when every warp of both passes covers one 32-site group of one parity: one site per thread, and
-// (for the parity-major order) a multiple of 32 sites per parity; the candidates fit the vote words.
-bool votes_ok(const LaunchCtx &lc, const Geom &g) {
+// The passes can keep and use per-group candidate lists when every warp of both passes covers one
+// 32-site group of one parity: one site per thread, and (for the parity-major order) a multiple of 32
+// sites per parity; the pruned candidates fit the list words.
+bool lists_ok(const LaunchCtx &lc, const Geom &g) {
     const bool aligned = (g.n_local_half & 31) == 0;
-    return lc.nt->npruned <= 32 * kVoteWords && lc.rho_apt == 1 && lc.force_apt == 1 && (lc.rho_order == 1 || aligned) &&
+    return lc.nt->npruned <= 32 * kListWords && lc.rho_apt == 1 && lc.force_apt == 1 && (lc.rho_order == 1 || aligned) &&
            (lc.force_order == 1 || aligned);
 }
 static void launch_lat_rho_threads(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook,
-                                   int tb, int te, bool votes = false) {
+                                   int tb, int te, bool lists = false) {
     const int order = lc.rho_order, b = lc.rho_block;
     const int n = (te - tb + b * lc.rho_apt - 1) / (b * lc.rho_apt);
     if (n <= 0) return;
@@ -962,7 +949,7 @@ static void launch_lat_rho_threads(const LaunchCtx &lc, const Geom &g, Slots s, 
         if (mixed) k_lat_rho_mixed<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, tb, te, false);
         else k_lat_rho_fp64<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, tb, te);
     } else {
-        if (mixed) k_lat_rho_mixed<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, tb, te, votes);
+        if (mixed) k_lat_rho_mixed<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, tb, te, lists);
         else k_lat_rho_fp64<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, hook, order, tb, te);
     }
 }
@@ -990,10 +977,10 @@ __global__ void __launch_bounds__(kSkinSlots) k_skin_advance(SkinState *k) {
 void launch_skin_advance(const LaunchCtx &lc, Slots s) { k_skin_advance<<<1, kSkinSlots, 0, lc.stream>>>(s.skin); }
 void launch_skin_dirty(const LaunchCtx &lc, Slots s) { cudaMemsetAsync(&s.skin->dirty, 1, 1, lc.stream); }
 
-// A voted mixed pass is followed by the skin's advance. A mixed pass without votes leaves the near
-// words behind the positions, so the next voted pass rebuilds them.
-void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook, bool votes) {
-    const bool v = votes && mixed && !hook && votes_ok(lc, g);
+// A mixed pass with the group lists is followed by the skin's advance. A mixed pass without them
+// leaves the lists behind the positions, so the next pass with them rebuilds them.
+void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook, bool lists) {
+    const bool v = lists && mixed && !hook && lists_ok(lc, g);
     launch_lat_rho_threads(lc, g, s, in, t, mixed, hook, 0, gather_threads(g, lc.rho_order), v);
     if (v) launch_skin_advance(lc, s);
     else if (mixed) launch_skin_dirty(lc, s);
@@ -1011,11 +998,11 @@ static void site_threads(const Geom &g, int order, int u0, int u1, int tb[2], in
     }
 }
 void launch_lat_rho_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, int u0, int u1,
-                          bool votes) {
+                          bool lists) {
     if (u1 <= u0) return;
     int tb[2], te[2], nr;
     site_threads(g, lc.rho_order, u0, u1, tb, te, nr);
-    const bool v = votes && mixed && votes_ok(lc, g);
+    const bool v = lists && mixed && lists_ok(lc, g);
     for (int r = 0; r < nr; r++) launch_lat_rho_threads(lc, g, s, in, t, mixed, false, tb[r], te[r], v);
     if (!v && mixed) launch_skin_dirty(lc, s);  // the caller advances the skin after the last slab
 }
@@ -1177,11 +1164,13 @@ __device__ __forceinline__ void force_sum_mixed(const NeighTables &nt, const Geo
 #pragma unroll 1  // 2, 3, 4 and full unrolling measured slower
     for (int q = q0; q < q1; q++) force_candidate<PAR>(nt, g, s, pt, si, ti, fbase, uixy, ui.z, dfi, q, sxy, sz);
 }
-// the pruned candidates the density pass of this step found inside the cutoff for some site of the
-// warp's group, in table order (the others are outside for every site: same displacements, same r^2)
+// the candidates of the warp's group list, in table order: the density pass of this step checked or
+// rebuilt the list, so it holds every pruned candidate inside the cutoff for any site of the group
+// (the cutoff is tested again here with the same rounding, so the pairs summed are those of the full
+// loop, in the same order)
 template <int PAR>
-__device__ __forceinline__ void force_sum_voted(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int si,
-                                                int ti, float4 ui, float dfi, const unsigned *words, f2 &sxy, float &sz) {
+__device__ __forceinline__ void force_sum_listed(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int si,
+                                                 int ti, float4 ui, float dfi, const unsigned *words, f2 &sxy, float &sz) {
     const int fbase = (ti * 3) * pt.nr;
     const f2 uixy = f2_pack(ui.x, ui.y);
     for (int k = 0; k * 32 < nt.npruned; k++)
@@ -1200,7 +1189,7 @@ __device__ __forceinline__ int local_index_of(const Geom &g, int sl, int &i, int
 
 __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables &nt, const Geom &g, const Slots &s, const Inter &in,
                                                 const PotTables &pt, StepParams *sp, bool kick, bool hook, int order,
-                                                bool fuse_next, bool votes) {
+                                                bool fuse_next, bool lists) {
     int par, u;
     const int sl = gather_site(g, t, order, par, u);
     if (sl < 0) return;
@@ -1221,10 +1210,10 @@ __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables 
     f2 sxy = f2_pack(0.f, 0.f);
     float sz = 0.f;
     const int np = nt.npruned;
-    if (votes) {  // the density pass of this step left the votes of this warp's group
-        const unsigned *w = group_words(g, s, par, u);
-        if (par) force_sum_voted<1>(nt, g, s, pt, si, ti, ui, dfi, w, sxy, sz);
-        else force_sum_voted<0>(nt, g, s, pt, si, ti, ui, dfi, w, sxy, sz);
+    if (lists) {
+        const unsigned *w = group_list(g, s, par, u);
+        if (par) force_sum_listed<1>(nt, g, s, pt, si, ti, ui, dfi, w, sxy, sz);
+        else force_sum_listed<0>(nt, g, s, pt, si, ti, ui, dfi, w, sxy, sz);
     } else {
         if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, 0, np, sxy, sz);
         else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, 0, np, sxy, sz);
@@ -1264,10 +1253,10 @@ __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables 
 template <bool LOOP>  // LOOP: several sites per thread, one grid stride apart
 __global__ void __launch_bounds__(512, 3) k_lat_force_mixed(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt,
                                                          StepParams *sp, bool kick, bool hook, int order, int tbase,
-                                                         int nthreads, bool fuse_next, bool votes) {
+                                                         int nthreads, bool fuse_next, bool lists) {
     const int t0 = tbase + blockIdx.x * blockDim.x + threadIdx.x;  // threads [tbase, nthreads)
     if (!LOOP) {
-        if (t0 < nthreads) k_lat_force_mixed_site(t0, nt, g, s, in, pt, sp, kick, hook, order, fuse_next, votes);
+        if (t0 < nthreads) k_lat_force_mixed_site(t0, nt, g, s, in, pt, sp, kick, hook, order, fuse_next, lists);
         return;
     }
     for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x)
@@ -1276,7 +1265,7 @@ __global__ void __launch_bounds__(512, 3) k_lat_force_mixed(const __grid_constan
 
 static void launch_lat_force_threads(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *p,
                                      bool kick, bool mixed, bool hook, int tb, int te, bool fuse_next = false,
-                                     bool votes = false) {
+                                     bool lists = false) {
     const int order = lc.force_order, b = lc.force_block;
     const int n = (te - tb + b * lc.force_apt - 1) / (b * lc.force_apt);
     if (n <= 0) return;
@@ -1285,21 +1274,21 @@ static void launch_lat_force_threads(const LaunchCtx &lc, const Geom &g, Slots s
         if (mixed) k_lat_force_mixed<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te, fuse, false);
         else k_lat_force_fp64<true><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te);
     } else {
-        if (mixed) k_lat_force_mixed<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te, fuse, votes);
+        if (mixed) k_lat_force_mixed<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te, fuse, lists);
         else k_lat_force_fp64<false><<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t, p, kick, hook, order, tb, te);
     }
 }
 void launch_lat_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *p, bool kick,
-                      bool mixed, bool hook, bool fuse_next, bool votes) {
+                      bool mixed, bool hook, bool fuse_next, bool lists) {
     launch_lat_force_threads(lc, g, s, in, t, p, kick, mixed, hook, 0, gather_threads(g, lc.force_order), fuse_next,
-                             votes && mixed && !hook && votes_ok(lc, g));
+                             lists && mixed && !hook && lists_ok(lc, g));
 }
 void launch_lat_force_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, StepParams *p, bool kick,
-                            bool mixed, int u0, int u1, bool votes) {
+                            bool mixed, int u0, int u1, bool lists) {
     if (u1 <= u0) return;
     int tb[2], te[2], nr;
     site_threads(g, lc.force_order, u0, u1, tb, te, nr);
-    const bool v = votes && mixed && votes_ok(lc, g);
+    const bool v = lists && mixed && lists_ok(lc, g);
     for (int r = 0; r < nr; r++) launch_lat_force_threads(lc, g, s, in, t, p, kick, mixed, false, tb[r], te[r], false, v);
 }
 
