@@ -201,7 +201,7 @@ mg_status mg_step_host(mg_context *ctx, mg_atom_element *atoms, int64_t n_slots,
 mg_status mg_set_step_fusion(mg_context *ctx, int32_t steps_per_graph);
 /* Number of z-slabs of mg_step_host's pipeline (default 16; 0 or 1: no pipelining). */
 mg_status mg_set_host_pipeline(mg_context *ctx, int32_t chunks);
-/* Verlet skin of the mixed form's candidate lists, in Angstrom (default 0.25; 0: off; at most a0).
+/* Verlet skin of the mixed form's candidate lists, in Angstrom (default 0.2; 0: off; at most a0).
  * Each group of 32 sites keeps the pruned candidates that some site of the group had within
  * rc + skin when the list was built. The density pass then visits only those, until the sum of the
  * per-step maximum displacements, doubled, reaches the skin; a record written by an upload or by

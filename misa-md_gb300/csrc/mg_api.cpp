@@ -131,10 +131,10 @@ cudaError_t dalloc(mg_context *ctx, T **p, size_t n) {
     return e;
 }
 
-// Verlet skin of the near words (mixed form), Angstrom. The group lists then hold about the sixth
-// shell besides the 58 neighbours inside the cutoff; at 600 K and dt = 1 fs they last about 10 steps
-// (0.2 to 0.3 A measured equally fast on 16M atoms).
-constexpr double kDefaultSkin = 0.25;
+// Verlet skin of the group candidate lists (mixed form), Angstrom. The lists then hold about the
+// sixth shell besides the 58 neighbours inside the cutoff; at 600 K and dt = 1 fs they last about 8
+// steps (0.15 to 0.25 A measured within 0.3% of each other on 16M atoms, 0.2 the fastest).
+constexpr double kDefaultSkin = 0.2;
 void set_skin(Geom &g, double skin) {
     g.skin_h = static_cast<float>(skin * g.inv_h);
     const double r = (g.rc + skin) * g.inv_h;
