@@ -67,7 +67,7 @@ struct Geom {
     float h_f;               // a0 / 2 (float)
     float rc2_h;             // (rc / h)^2 in half-lattice units
     float rc2_pre;           // rc2_h * (1 + 1e-4): FP32 candidate test of the FP64 gathers
-    float skin_h;            // Verlet skin of the near words, half-lattice units (0: off)
+    float skin_h;            // Verlet skin of the group candidate lists, half-lattice units (0: off)
     float rcs2_h;            // ((rc + skin) / h)^2 (rc2_h when the skin is off)
     // site_half[m] = RN((m / 2) a0), m in [0, n_site_half): the coordinate of half-lattice index m,
     // rounded as the site formula of decide rounds it (x: m = i; y, z: m = 2j + parity)
@@ -76,19 +76,20 @@ struct Geom {
 };
 
 // Verlet skin on the group candidate lists (mixed form). The density pass of some step built the
-// near words from the displacement records of that step. Until `dirty` is set, no record has changed
-// since then except through firststep, and every change of a record is at most the maximum change
-// of its step (the step_max2 words); acc sums those maxima since the build. A pair inside rc now
-// was therefore inside rc + 2 acc when the words were built, and while 2 acc stays below the skin the
-// near words hold every pair inside the cutoff.
+// lists from the displacement records of that step. Until `dirty` is set, no record has changed since
+// then except through firststep (or through recombination, whose neighbourhood marks make the groups
+// that can see the atom rebuild their own lists), and every change of a record is at most the
+// maximum change of its step (the step_max2 words); acc sums those maxima since the build. A pair
+// inside rc now was therefore inside rc + 2 acc when the lists were built, and while 2 acc stays
+// below the skin the lists hold every pair inside the cutoff.
 struct SkinState {
     unsigned step_max2[kSkinSlots];  // this step's max |du|^2 (float bits, half-lattice units)
     float acc;                       // the sum of the per-step maxima of |du| since the build
     int dirty;                       // a record changed outside firststep: the next pass rebuilds
-    int rebuilt;                     // the last density pass rebuilt the near words
+    int rebuilt;                     // the last density pass rebuilt every group's list
     int pad;
-    unsigned long long rebuilds;     // density passes that rebuilt the near words
-    unsigned long long passes;       // density passes with near words
+    unsigned long long rebuilds;     // density passes that rebuilt every group's list
+    unsigned long long passes;       // density passes with the group lists
 };
 
 // Lattice slot arrays (structure of arrays over every slot, ghosts included).
@@ -270,10 +271,10 @@ void launch_lat_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTa
 void launch_lat_rho_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, int u0, int u1,
                           bool lists = false);
 bool lists_ok(const LaunchCtx &lc, const Geom &g);
-// after the density pass of a step that used the near words, before the next firststep: fold the
+// after the density pass of a step that used the group lists, before the next firststep: fold the
 // step's maximum displacement into the skin's sum (or restart it when the pass rebuilt the words)
 void launch_skin_advance(const LaunchCtx &lc, Slots s);
-// a displacement record changed outside firststep: the next density pass rebuilds the near words
+// a displacement record changed outside firststep: the next density pass rebuilds every group's list
 void launch_skin_dirty(const LaunchCtx &lc, Slots s);
 // forward df for the ghost slots inside local planes [k0, k1), or (k0 < 0) the ghost planes below and
 // above the box plus the ghost inter atoms

@@ -409,7 +409,7 @@ def test_autotune_keeps_results_bit_identical(pkg, wl, potentials, gpu_lib, prec
             assert t["rho_order"] in (0, 1) and t["force_block"] in (128, 256, 512) and t["force_apt"] in (1, 2, 4)
         elif tune is not None:
             ctx.set_tuning(*tune)
-        ctx.simulate(20)  # mixed: a fused 16-body graph; (1, 128, 1, 512) takes the density-pass votes
+        ctx.simulate(20)  # mixed: a fused 16-body graph; (1, 128, 1, 512) walks the group candidate lists
         got, _ = ctx.download()
         runs.append(got)
         ctx.close()

@@ -37,7 +37,7 @@ def mixed_ctx(pkg, cells, pot, atoms, skin, dt=0.001, inter_capacity=0):
     ctx = pkg.Context(cells, A0, RCF, precision="mixed", inter_capacity=inter_capacity)
     ctx.pot_init_setfl(pot)
     ctx.set_timestep(dt)
-    ctx.set_tuning(1, 256, 1, 256)  # warp-interleaved parities: votes for any box size
+    ctx.set_tuning(1, 256, 1, 256)  # warp-interleaved parities: group lists for any box size
     ctx.set_neighbour_skin(skin)
     ctx.upload(atoms)
     ctx.prepare()
