@@ -10,6 +10,7 @@
 // result must be reproduced bit for bit: velocity-Verlet, the decide distance test, the
 // Wigner-Seitz mapping, ghost shifts and setv.
 
+#include <algorithm>
 #include <climits>
 #include <cstddef>
 #include <cstdio>
@@ -360,11 +361,12 @@ void launch_site_table(const LaunchCtx &lc, const Geom &g, double *site_half) {
 }
 
 // Displaced slots are recorded in scan order without a sort: firststep writes one byte per local slot
-// (thread t holds local slot t in k, j, i order; 1 = displaced). A count kernel sums the bytes of each
+// (byte t for local index t, in k, j, i order; 1 = displaced). A count kernel sums the bytes of each
 // group of kFirstThreads slots, a one-block scan turns the sums into offsets, and a collect kernel
 // writes the slots in order. firststep keeps its early exits and needs no warp or block collective.
 // decide's distance test (src/atom.cpp:34-42) with each operation rounded on its own; a displaced
 // atom also counts itself into CNT_DISP_RAW, so the collection kernels can skip steps without any
+// displaced atom.
 __device__ __noinline__ bool exact_displaced(double ex, double ey, double ez, double thr, int *raw_count) {
     double dist = __dmul_rn(ex, ex);
     dist = __dadd_rn(dist, __dmul_rn(ey, ey));
@@ -437,25 +439,27 @@ __device__ __forceinline__ void first_half(const Geom &g, const Slots &s, const 
 // alternates between are always complete.
 // alt: inside a graph whose bodies alternate their u4 buffers, where the previous body's records are
 // in s.u4n
+// A grid-stride loop over a grid of a few blocks per SM: a fused body's launch, which returns at once,
+// then costs one small launch instead of a grid over every slot.
 template <bool MOVE, bool DECIDE>
 __global__ void __launch_bounds__(kFirstThreads) k_firststep(Geom g, Slots s, Inter in, const StepParams *__restrict__ p,
                                                              int t0, int t1, bool fused, bool alt) {
-    const int t = t0 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= t1) return;
     if (fused && lattice_only(in)) return;
-    int i, j, k;
-    const int sl = local_slot(g, t, i, j, k);
-    const int ty = s.type[sl];
-    if (ty < 0) {
-        if (DECIDE) in.dflag[t] = 0;
-        if (MOVE) s.u4[sidx(g, sl)] = vacant_u4();
-        return;
+    for (int t = t0 + blockIdx.x * blockDim.x + threadIdx.x; t < t1; t += gridDim.x * blockDim.x) {
+        int i, j, k;
+        const int sl = local_slot(g, t, i, j, k);
+        const int ty = s.type[sl];
+        if (ty < 0) {
+            if (DECIDE) in.dflag[t] = 0;
+            if (MOVE) s.u4[sidx(g, sl)] = vacant_u4();
+            continue;
+        }
+        if (MOVE)
+            first_half<true, DECIDE>(g, s, in, p, sl, t, i, j, k, ty, s.vx[sl], s.vy[sl], s.vz[sl], s.fx[sl], s.fy[sl],
+                                     s.fz[sl], s.u4, alt ? s.u4n : s.u4);
+        else
+            first_half<false, DECIDE>(g, s, in, p, sl, t, i, j, k, ty, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, s.u4, s.u4);
     }
-    if (MOVE)
-        first_half<true, DECIDE>(g, s, in, p, sl, t, i, j, k, ty, s.vx[sl], s.vy[sl], s.vz[sl], s.fx[sl], s.fy[sl],
-                                 s.fz[sl], s.u4, alt ? s.u4n : s.u4);
-    else
-        first_half<false, DECIDE>(g, s, in, p, sl, t, i, j, k, ty, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, s.u4, s.u4);
 }
 
 // one warp per group of kFirstThreads flag bytes (8 per lane, read as one 64-bit word): its count
@@ -469,39 +473,41 @@ __global__ void k_disp_count(Inter in, int nblocks) {
     if ((threadIdx.x & 31) == 0) in.dblock[b] = c;
 }
 
-// one block: counts a[0..n) -> base + exclusive offsets (in place); returns base + the total (every thread)
+// one block: counts a[0..n) -> base + exclusive offsets (in place); returns base + the total (every
+// thread). Each thread takes one contiguous chunk: a pass summing it, one block scan of the chunk
+// sums, and a pass writing the chunk's offsets (one scan instead of one per blockDim.x counts).
 __device__ int block_scan_counts(int *a, int n, int base) {
     __shared__ int warp_tot[32];
-    __shared__ int running;
-    if (threadIdx.x == 0) running = base;
-    __syncthreads();
-    for (int c0 = 0; c0 < n; c0 += blockDim.x) {
-        const int b = c0 + threadIdx.x;
-        const int v = b < n ? a[b] : 0;
-        int x = v;  // inclusive warp scan
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, x, o);
-            if ((threadIdx.x & 31) >= o) x += y;
-        }
-        if ((threadIdx.x & 31) == 31) warp_tot[threadIdx.x >> 5] = x;
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            int w = threadIdx.x < (blockDim.x >> 5) ? warp_tot[threadIdx.x] : 0;
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, w, o);
-                if (threadIdx.x >= o) w += y;
-            }
-            warp_tot[threadIdx.x] = w;  // inclusive over warps
-        }
-        __syncthreads();
-        const int warp_base = (threadIdx.x >> 5) ? warp_tot[(threadIdx.x >> 5) - 1] : 0;
-        const int cur = running;
-        if (b < n) a[b] = cur + warp_base + x - v;
-        __syncthreads();
-        if (threadIdx.x == 0) running = cur + warp_tot[(blockDim.x >> 5) - 1];
-        __syncthreads();
+    const int per = (n + (int) blockDim.x - 1) / (int) blockDim.x;
+    const int b0 = min(n, (int) threadIdx.x * per), b1 = min(n, b0 + per);
+    int v = 0;
+#pragma unroll 4
+    for (int b = b0; b < b1; b++) v += a[b];
+    int x = v;  // inclusive warp scan of the chunk sums
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) >= o) x += y;
     }
-    return running;
+    if ((threadIdx.x & 31) == 31) warp_tot[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int w = threadIdx.x < (blockDim.x >> 5) ? warp_tot[threadIdx.x] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (threadIdx.x >= o) w += y;
+        }
+        warp_tot[threadIdx.x] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    int run = base + ((threadIdx.x >> 5) ? warp_tot[(threadIdx.x >> 5) - 1] : 0) + x - v;
+    for (int b = b0; b < b1; b++) {
+        const int c = a[b];
+        a[b] = run;
+        run += c;
+    }
+    const int total = base + warp_tot[(blockDim.x >> 5) - 1];
+    __syncthreads();  // warp_tot is free again for a later call
+    return total;
 }
 
 // one block: block counts -> exclusive offsets (in place), total -> CNT_DISPLACED (clamped to dcap)
@@ -547,12 +553,12 @@ void launch_firststep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, con
                       int t1, bool fused, bool alt) {
     if (t1 < 0) t1 = g.n_local;
     if (t1 <= t0) return;
-    const int b = kFirstThreads, n = (t1 - t0 + b - 1) / b;
+    const int b = kFirstThreads, n = std::min((t1 - t0 + b - 1) / b, lc.num_sms * 8);
     if (decide) k_firststep<true, true><<<n, b, 0, lc.stream>>>(g, s, in, p, t0, t1, fused, alt);
     else k_firststep<true, false><<<n, b, 0, lc.stream>>>(g, s, in, p, t0, t1, fused, alt);
 }
 void launch_decide_scan(const LaunchCtx &lc, const Geom &g, Slots s, Inter in) {
-    const int b = kFirstThreads, n = (g.n_local + b - 1) / b;
+    const int b = kFirstThreads, n = std::min((g.n_local + b - 1) / b, lc.num_sms * 8);
     k_firststep<false, true><<<n, b, 0, lc.stream>>>(g, s, in, nullptr, 0, g.n_local, false, false);
 }
 void launch_displaced_collect(const LaunchCtx &lc, const Geom &g, Inter in) {
