@@ -64,8 +64,8 @@ mg_status mg_env_clean(void);
 
 /* ---------------------------------------------------------------------------------------------
  * Context: replaces cuda_domain_init(const comm::BccDomain*) (src/arch/arch_imp.h:21, called at
- * src/simulation.cpp:126-128). One rank owning the whole periodic box: phase_space unit cells per
- * dimension, ghost width ceil(cutoff_radius_factor)+1 (src/simulation.cpp:120), cutoff radius
+ * src/simulation.cpp:52-54). One rank owning the whole periodic box: phase_space unit cells per
+ * dimension, ghost width ceil(cutoff_radius_factor)+1 (src/simulation.cpp:46), cutoff radius
  * lattice_const * cutoff_radius_factor (src/atom.cpp:14-19). Every dimension must be at least
  * 2 * ghost cells. precision: MG_PREC_FP64 or MG_PREC_MIXED. inter_capacity: maximum local
  * inter-atom count (0 picks a default).
@@ -81,7 +81,7 @@ mg_status mg_set_precision(mg_context *ctx, int32_t precision);
 
 /* ---------------------------------------------------------------------------------------------
  * Neighbour offsets: replaces cuda_nei_offset_init(const NeighbourIndex<AtomElement>*)
- * (src/arch/arch_imp.h:23, called at src/simulation.cpp:141-143). The context builds its own
+ * (src/arch/arch_imp.h:23, called at src/simulation.cpp:67-69). The context builds its own
  * tables at mg_create; this entry point checks the host's four tables against them (same entries,
  * same order) and returns MG_ERR_ARG on any difference.
  * ------------------------------------------------------------------------------------------- */
@@ -92,7 +92,7 @@ mg_status mg_nei_offset_init(mg_context *ctx, const int64_t *full_even, const in
 mg_status mg_nei_offsets(const mg_context *ctx, int32_t which, int64_t *out, int32_t cap, int32_t *n);
 
 /* ---------------------------------------------------------------------------------------------
- * Potential: replaces cuda_pot_init(eam*) (src/arch/arch_imp.h:25, called at src/simulation.cpp:207
+ * Potential: replaces cuda_pot_init(eam*) (src/arch/arch_imp.h:25, called at src/simulation.cpp:133
  * after interpolateFile). Either a setfl file, or the parsed tables (F[e][nrho], rho[e][nr],
  * r*phi[pair][nr] for pairs i>=j in lower-triangle order). atomic_numbers map atom types
  * Fe/Cu/Ni (keys 26/29/28, src/types/atom_types.h:61-73) to table elements.
@@ -122,7 +122,7 @@ mg_status mg_eam_df_calc(mg_context *ctx, mg_atom_element *atoms, double cutoff_
 mg_status mg_eam_force_calc(mg_context *ctx, mg_atom_element *atoms, double cutoff_radius);
 
 /* ---------------------------------------------------------------------------------------------
- * Resident state: the whole step of simulation::simulate (src/simulation.cpp:238-268) on the GPU,
+ * Resident state: the whole step of simulation::simulate (src/simulation.cpp:164-194) on the GPU,
  * state kept in HBM between calls.
  * ------------------------------------------------------------------------------------------- */
 /* Upload the slot array (n_slots records, reference index order) and the inter-atom list. */
@@ -144,9 +144,9 @@ mg_status mg_set_variable_timestep(mg_context *ctx, double dx_max, double dt_min
 mg_status mg_clock(mg_context *ctx, int64_t *steps, double *time_ps, double *dt_ps);
 /* The dt of the most recent min(steps, cap, 65536) steps, oldest first; *n_out = how many. Syncs. */
 mg_status mg_dt_history(mg_context *ctx, double *out, int64_t cap, int64_t *n_out);
-/* simulation::prepareForStart body (src/simulation.cpp:209-219): first ghost exchange, computeEam. */
+/* simulation::prepareForStart body (src/simulation.cpp:137-145): first ghost exchange, computeEam. */
 mg_status mg_prepare(mg_context *ctx);
-/* nsteps iterations of the loop body (src/simulation.cpp:241-265): firststep, decide, exchangeInter,
+/* nsteps iterations of the loop body (src/simulation.cpp:165-193): firststep, decide, exchangeInter,
  * borderInter, exchangeAtom, computeEam, secondstep. Asynchronous on the context stream unless
  * sync != 0. The step sequence is captured once as a CUDA graph and replayed; in the mixed form with
  * a fixed dt, runs of 16 bodies replay one fused graph (mg_set_step_fusion). */
@@ -154,14 +154,14 @@ mg_status mg_simulate(mg_context *ctx, int64_t nsteps, int32_t sync);
 /* One phase of the loop body, for parity checks: 0 firststep, 1 decide, 2 exchangeInter,
  * 3 borderInter, 4 exchangeAtom, 5 computeEam, 6 secondstep. */
 mg_status mg_phase(mg_context *ctx, int32_t phase);
-/* simulation::collisionStep (src/simulation.cpp:282-291): atom::setv on the slot at
+/* simulation::collisionStep (src/simulation.cpp:208-217): atom::setv on the slot at
  * lat = (cell x, cell y, cell z, basis) (src/atom.cpp:475-494), exchanges, computeEam. */
 mg_status mg_collision_step(mg_context *ctx, const int32_t lat[4], const double dir[3], double energy_ev);
-/* configuration::rescale (src/system_configuration.cpp:321-346) with n_atoms for the degrees of freedom. */
+/* configuration::rescale (src/system_configuration.cpp:86-111) with n_atoms for the degrees of freedom. */
 mg_status mg_rescale(mg_context *ctx, double t_set, uint64_t n_atoms);
 
 typedef struct mg_thermo_out {
-    double mvv;               /* sum m v^2 (src/system_configuration.cpp:296-319) */
+    double mvv;               /* sum m v^2 (src/system_configuration.cpp:61-84) */
     double kinetic_energy;    /* mvv / 2 */
     double potential_energy;  /* sum F(rho_i) + 1/2 sum phi_ij (extension; only when requested) */
     double force_sum[3];      /* configuration::systemForce (src/system_configuration.cpp:8-24) */
@@ -290,7 +290,7 @@ void *mg_batch_stream(const mg_batch *b);
 const char *mg_batch_last_error(const mg_batch *b);
 mg_status mg_batch_destroy(mg_batch *b);
 
-/* ---- Creation mode (simulation::createAtoms with create_mode, src/simulation.cpp:57-84 ->
+/* ---- Creation mode (simulation::createAtoms with create_mode, src/simulation.cpp:58-85 ->
  * WorldBuilder::build, src/world_builder.cpp:64-199), host only ----
  * Fills a host slot array (n_slots = the grid of mg_grid for this box) with the reference's
  * created crystal: ids 1..N in k, j, i order, types drawn with the C library's rand() in its

@@ -1,6 +1,6 @@
 // C ABI of libmisa_gb300.so: context lifetime, device state, potential upload, the per-step kernel
 // sequence (captured once as a CUDA graph), the reference's per-phase hooks and the thermo reductions.
-// The call order of one step follows simulation::simulate (src/simulation.cpp:238-268).
+// The call order of one step follows simulation::simulate (src/simulation.cpp:164-194).
 
 #include <algorithm>
 #include <cmath>
@@ -240,7 +240,7 @@ void seq_step(mg_context *ctx, Timer *t, bool fused_prev = false, bool fuse_next
 }
 // steps of mg_simulate that run fused: the mixed form with a fixed dt
 bool fusable(const mg_context *ctx) { return ctx->fuse_steps >= 2 && ctx->mixed() && ctx->dx_max <= 0.0; }
-constexpr int kLaunchesPerStep = 18;
+constexpr int kLaunchesPerStep = 20;
 
 mg_status require_ready(mg_context *ctx) {
     if (!ctx->pot_ready) { ctx->err = "potential not initialised"; return MG_ERR_POTENTIAL; }
@@ -470,7 +470,7 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     if (!out || !phase_space || !(lattice_const > 0) || !(rcf > 0)) { g_create_error = "bad argument"; return MG_ERR_ARG; }
     if (precision != MG_PREC_FP64 && precision != MG_PREC_MIXED) { g_create_error = "bad precision"; return MG_ERR_ARG; }
     *out = nullptr;
-    const int ghost = static_cast<int>(std::ceil(rcf)) + 1;       // src/simulation.cpp:120
+    const int ghost = static_cast<int>(std::ceil(rcf)) + 1;       // src/simulation.cpp:46
     const int cut_lattice = static_cast<int>(std::ceil(rcf));      // libcomm cut_lattice
     for (int d = 0; d < 3; d++) {
         if (phase_space[d] < 2 * ghost) { g_create_error = "every dimension needs at least 2*ghost unit cells"; return MG_ERR_ARG; }
@@ -581,6 +581,10 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     ALLOC(in.far_flag, ns);
     ALLOC(in.bucket, (size_t) nbuck);
     ALLOC(in.n_bucket, 1);
+    // every local inter atom lists at most its nearest site and the full offsets of that site
+    in.tcap = static_cast<int>(std::min<int64_t>(g.n_local, static_cast<int64_t>(in.cap) * (kMaxFull + 1)));
+    ALLOC(in.touch_bits, ns / 32 + 1);
+    ALLOC(in.touched, (size_t) in.tcap);
     ctx->n_partials = ctx->num_sms * 4;
     ALLOC(ctx->d_partials, (size_t) ctx->n_partials * 8);
     ALLOC(ctx->d_thermo, 8);
@@ -596,6 +600,7 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     if (e == cudaSuccess) e = cudaMemsetAsync(in.claim, 0x7f, ns * sizeof(int), ctx->stream);  // 0x7f7f7f7f > any list index
     if (e == cudaSuccess) e = cudaMemsetAsync(in.far_flag, 0, ns, ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(in.n_bucket, 0, sizeof(int), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(in.touch_bits, 0, (ns / 32 + 1) * sizeof(unsigned), ctx->stream);
     if (e == cudaSuccess)  // the padding past n_local is never written and must read as "not displaced"
         e = cudaMemsetAsync(in.dflag, 0, ((static_cast<size_t>(g.n_local) + kFirstThreads - 1) / kFirstThreads) * kFirstThreads,
                             ctx->stream);
@@ -904,7 +909,7 @@ mg_status mg_prepare(mg_context *ctx) {
     if (!ctx) return MG_ERR_ARG;
     mg_status st = require_ready(ctx);
     if (st != MG_OK) return st;
-    // exchangeAtomFirst, clearForce, computeEam (src/simulation.cpp:209-219); the lattice passes assign
+    // exchangeAtomFirst, clearForce, computeEam (src/simulation.cpp:137-145); the lattice passes assign
     // instead of accumulate, which is what clearForce + accumulate gives
     seq_compute_eam(ctx, false, false, 0, nullptr);
     if ((st = check_launch(ctx)) != MG_OK) return st;
@@ -999,7 +1004,7 @@ mg_status mg_phase(mg_context *ctx, int32_t phase) {
     return status_from_bits(ctx, bits);
 }
 
-// simulation::collisionStep (src/simulation.cpp:282-291) enqueued on the context's stream
+// simulation::collisionStep (src/simulation.cpp:208-217) enqueued on the context's stream
 static mg_status enqueue_collision(mg_context *ctx, const int32_t lat[4], const double dir[3], double energy) {
     // atom::setv bounds (src/atom.cpp:477-482), one rank: the sub-box starts at 0
     const Geom &g = ctx->g;

@@ -27,7 +27,12 @@ constexpr uint32_t kInBox = 0, kXLow = 1u, kXHigh = 2u, kYLow = 4u, kYHigh = 8u,
 
 // device counters / flags word indices
 // CNT_DISP_RAW: displaced slots counted by firststep this step (0 lets the collection kernels skip)
-enum { CNT_INTER = 0, CNT_GHOST = 1, CNT_DISPLACED = 2, CNT_ERRORS = 3, CNT_FAR = 4, CNT_DISP_RAW = 5, CNT_WORDS = 8 };
+// CNT_TOUCHED: lattice owners listed by an inter-atom pass for the ordered owner gather that follows;
+// CNT_TOUCH_DONE: blocks of that gather finished (the last one resets both words)
+enum {
+    CNT_INTER = 0, CNT_GHOST = 1, CNT_DISPLACED = 2, CNT_ERRORS = 3, CNT_FAR = 4, CNT_DISP_RAW = 5, CNT_TOUCHED = 6,
+    CNT_TOUCH_DONE = 7, CNT_WORDS = 8
+};
 
 inline double atom_mass(int type) {  // src/types/atom_types.h:42-53
     switch (type) {
@@ -139,6 +144,12 @@ struct Inter {
     // buckets: sorted (key, ref) pairs; ref < cap: local index, else cap + ghost index
     long long *bucket;       // (key << 32) | ref packed, sorted ascending
     int *n_bucket;
+    // lattice owners with an inter atom inside the cutoff: one bit per slot (all clear between
+    // passes) and the list of owners whose bit an inter-atom pass set, in any order; the owner
+    // gather that follows sums each owner's inter-atom terms in a fixed order and clears the bits
+    unsigned *touch_bits;
+    int *touched;
+    int tcap;
 };
 
 // One FP64 spline knot record (32 bytes, read as two 16-byte loads).

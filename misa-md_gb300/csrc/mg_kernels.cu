@@ -3,8 +3,9 @@
 // Layout: structure-of-arrays over the reference's ghost-extended slot grid (doubled x), one thread
 // per local slot. The lattice density and force passes are full-neighbour gathers over the offset
 // table pruned to sites that can lie inside the cutoff (no Newton-3 scatter, no reverse fold, no
-// atomics); inter atoms (few) keep the reference's structure and add their Newton-3 share to the
-// owning lattice slot with FP64 atomics. The periodic ghost copy replaces the MPI halo exchange.
+// atomics); inter atoms (few) keep the reference's structure for their own sums, and the lattice
+// owners they touch gather their Newton-3 shares in a fixed order. The periodic ghost copy replaces
+// the MPI halo exchange.
 //
 // Exact-rounding intrinsics (__dadd_rn / __dmul_rn / __ddiv_rn) are used wherever the reference's
 // result must be reproduced bit for bit: velocity-Verlet, the decide distance test, the
@@ -1840,7 +1841,11 @@ void launch_inter_manage(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, 
 
 // ------------------------------------------------------------------------------------------------
 // inter-atom EAM (atom::interRho / interForce, src/atom.cpp:194-284, 360-473), FP64 arithmetic.
-// One warp per local inter atom; Newton-3 shares go to the owning lattice slot by FP64 atomics.
+// One warp per local inter atom sums the atom's own terms. The Newton-3 shares that the reference
+// scatters into lattice atoms (and folds from ghost slots into their owners) are summed instead by
+// the owners themselves, in a fixed order, so every run gives the same bits: the inter-atom pass
+// lists each lattice owner it finds inside the cutoff, and an owner gather over that list adds the
+// owner's inter-atom terms in offset order, then bucket order.
 // ------------------------------------------------------------------------------------------------
 __device__ __forceinline__ int bucket_begin(const Inter &in, int nb, int key) {
     int lo = 0, hi = nb;
@@ -1897,11 +1902,25 @@ __device__ __forceinline__ double lat_df(const Geom &g, const Slots &s, int sl, 
 // kind: 0 density, 1 force, 2 energy
 // One warp per inter atom (the lists hold a few to thousands of atoms, each with ~460 partner
 // entries): the lanes share the 229 lattice entries and the 229 bucket keys of the atom's nearest
-// site, keep partial sums, and reduce them by shuffles in a fixed order. Shares that belong to
-// lattice atoms go to their owning slots with FP64 atomics, as the reference's Newton-3 scatter.
+// site, keep partial sums, and reduce them by shuffles in a fixed order. Every lattice owner with a
+// partner inside the cutoff is listed once (touch_owner) for k_inter_owner, which adds the owner's
+// share of the pair terms.
 __device__ __forceinline__ double warp_sum_d(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
+}
+// lists a lattice owner for the owner gather: the first caller to set its bit appends it
+__device__ __forceinline__ void touch_owner(Inter &in, int own) {
+    const unsigned bit = 1u << (own & 31);
+    if (atomicOr(&in.touch_bits[own >> 5], bit) & bit) return;
+    const int q = atomicAdd(&in.cnt[CNT_TOUCHED], 1);
+    if (q < in.tcap) in.touched[q] = own;
+    else set_error(in, MG_DEVERR_INTER_OVERFLOW);
+}
+// a slot of the local box (not a ghost slot)
+__device__ __forceinline__ bool is_local_slot(const Geom &g, int sl) {
+    const int X = sl % g.Sx, r = sl / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
+    return X >= g.gx && X < g.gx + g.bx && Y >= g.gy && Y < g.gy + g.by && Z >= g.gz && Z < g.gz + g.bz;
 }
 template <int KIND>
 __global__ void __launch_bounds__(128) k_inter_eam(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool mixed) {
@@ -1928,20 +1947,14 @@ __global__ void __launch_bounds__(128) k_inter_eam(const __grid_constant__ Neigh
             const double dx = xa - s.x[sj], dy = ya - s.y[sj], dz = za - s.z[sj];
             const double r2 = dx * dx + dy * dy + dz * dz;
             if (!(r2 < g.rc2)) continue;
-            const int own = owner_slot(g, sj);
+            touch_owner(in, owner_slot(g, sj));
             if (KIND == 0) {
                 acc += rho_fn(pt, tj, r2);
-                atomicAdd(&s.rho[own], rho_fn(pt, ta, r2));
             } else if (KIND == 1) {
                 const double fp = to_force(pt, ta, tj, r2, dfa, lat_df(g, s, sj, mixed));
                 fx += dx * fp; fy += dy * fp; fz += dz * fp;
-                atomicAdd(&s.fx[own], -dx * fp);
-                atomicAdd(&s.fy[own], -dy * fp);
-                atomicAdd(&s.fz[own], -dz * fp);
             } else {
-                const double h = 0.5 * pair_fn(pt, ta, tj, r2);
-                acc += h;
-                atomicAdd(&s.e[own], h);
+                acc += 0.5 * pair_fn(pt, ta, tj, r2);
             }
         }
         // inter partners: same-site bucket (not itself), then the buckets of the full offsets
@@ -1984,14 +1997,90 @@ __global__ void __launch_bounds__(128) k_inter_eam(const __grid_constant__ Neigh
         }
     }
 }
+// The lattice owners' side of the inter-atom pairs. One warp per owner listed by k_inter_eam: the
+// lanes walk the owner's site and its full offsets (reference order) and, per site, the bucket of
+// inter atoms whose nearest site it is (local atoms, and the ghost images borderInter made of atoms
+// near the far side of the box). Each pair inside the cutoff adds the term the inter atom's pass
+// would have scattered, computed from the same oriented difference x_inter - x_lattice; the lanes'
+// partial sums are reduced by shuffles in a fixed order and added to the owner once. Whether a ghost
+// lattice slot or a ghost inter atom carries the periodic image changes only the rounding of the
+// difference. A local inter atom whose nearest site is outside the box takes no part, as in the
+// inter-atom pass. The last block to finish resets the list for the next pass; the bits are clear by
+// then.
+template <int KIND>
+__global__ void __launch_bounds__(128) k_inter_owner(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool mixed) {
+    const int n = min(in.cnt[CNT_TOUCHED], in.tcap);
+    const int nb = *in.n_bucket;
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < n; w += warps) {  // warp-uniform
+        const int j = in.touched[w];
+        const int tj = s.type[j];
+        const double xj = s.x[j], yj = s.y[j], zj = s.z[j];
+        const double dfj = KIND == 1 ? lat_df(g, s, j, mixed) : 0.0;
+        const int par = (j % g.Sx) & 1;
+        const int nf = nt.nfull;
+        double acc = 0.0, fx = 0.0, fy = 0.0, fz = 0.0;
+        if (tj >= 0) {
+            for (int q = lane - 1; q < nf; q += 32) {
+                const int key = q < 0 ? j : j + (par ? nt.full[1][q] : nt.full[0][q]);
+                for (int b = bucket_begin(in, nb, key); b < nb && (int) (in.bucket[b] >> 32) == key; b++) {
+                    const int ref = (int) (in.bucket[b] & 0xffffffffLL);
+                    if (ref < in.cap && !is_local_slot(g, key)) continue;
+                    const InterRef o = inter_ref(in, ref);
+                    const double dx = o.x - xj, dy = o.y - yj, dz = o.z - zj;
+                    const double r2 = dx * dx + dy * dy + dz * dz;
+                    if (!(r2 < g.rc2)) continue;
+                    if (KIND == 0) {
+                        acc += rho_fn(pt, o.type, r2);
+                    } else if (KIND == 1) {
+                        const double fp = to_force(pt, o.type, tj, r2, o.df, dfj);
+                        fx += -dx * fp; fy += -dy * fp; fz += -dz * fp;
+                    } else {
+                        acc += 0.5 * pair_fn(pt, o.type, tj, r2);
+                    }
+                }
+            }
+        }
+        if (KIND == 1) {
+            fx = warp_sum_d(fx);
+            fy = warp_sum_d(fy);
+            fz = warp_sum_d(fz);
+        } else {
+            acc = warp_sum_d(acc);
+        }
+        if (lane == 0) {
+            if (tj >= 0) {
+                if (KIND == 0) s.rho[j] += acc;
+                else if (KIND == 1) { s.fx[j] += fx; s.fy[j] += fy; s.fz[j] += fz; }
+                else s.e[j] += acc;
+            }
+            atomicAnd(&in.touch_bits[j >> 5], ~(1u << (j & 31)));
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&in.cnt[CNT_TOUCH_DONE], 1) == (int) gridDim.x - 1) {
+            in.cnt[CNT_TOUCHED] = 0;
+            in.cnt[CNT_TOUCH_DONE] = 0;
+            __threadfence();
+        }
+    }
+}
+template <int KIND>
+void launch_inter_kind(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
+    k_inter_eam<KIND><<<lc.num_sms * 4, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
+    k_inter_owner<KIND><<<lc.num_sms * 4, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
+}
 void launch_inter_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
-    k_inter_eam<0><<<lc.num_sms * 4, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
+    launch_inter_kind<0>(lc, g, s, in, t, mixed);
 }
 void launch_inter_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
-    k_inter_eam<1><<<lc.num_sms * 4, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
+    launch_inter_kind<1>(lc, g, s, in, t, mixed);
 }
 void launch_inter_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
-    k_inter_eam<2><<<lc.num_sms * 4, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
+    launch_inter_kind<2>(lc, g, s, in, t, mixed);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -2050,7 +2139,7 @@ void launch_setv(const LaunchCtx &lc, const Geom &g, Slots s, int64_t slot, cons
     k_setv<<<1, 1, 0, lc.stream>>>(s, (int) slot, dir[0], dir[1], dir[2], energy);
 }
 
-// rescale (src/system_configuration.cpp:321-346): factor = sqrt(T / T_now) from the mvv reduction
+// rescale (src/system_configuration.cpp:86-111): factor = sqrt(T / T_now) from the mvv reduction
 __global__ void k_rescale(Geom g, Slots s, Inter in, const double *mvv, double t_set, uint64_t n_atoms) {
     const uint64_t dof = 3 * n_atoms - 3;
     const double scalar = __ddiv_rn(__dmul_rn(*mvv, kMvv2e), __dmul_rn((double) dof, kBoltz));

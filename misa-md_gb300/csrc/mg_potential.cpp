@@ -1,6 +1,6 @@
 // Host side of the potential: setfl parsing and the FP64 spline coefficient build, plus the neighbour
 // offset tables. This is the boundary of the external pot v0.1.0 library that MISA-MD calls
-// (SetflParser / eam::interpolateFile at src/simulation.cpp:161-205); its source is not part of the
+// (SetflParser / eam::interpolateFile at src/simulation.cpp:105-131); its source is not part of the
 // MISA-MD tree, so the published setfl format and interpolation scheme are implemented here:
 //   setfl: 3 comment lines; "N el1 .. elN"; "nrho drho nr dr cutoff"; per element "Z mass a0 lattice",
 //          F(rho) on nrho knots, rho(r) on nr knots; then r*phi(r) for pairs i >= j (lower triangle).

@@ -93,7 +93,7 @@ struct Uniform<LegacyRand> {
 template <class U>
 void build_world(const int64_t ps[3], double a0, double rcf, double t_set, uint32_t seed, const int32_t ratio[3],
                  mg_atom_element *atoms) {
-    const int64_t g = static_cast<int64_t>(std::ceil(rcf)) + 1;  // src/simulation.cpp:120
+    const int64_t g = static_cast<int64_t>(std::ceil(rcf)) + 1;  // src/simulation.cpp:46
     const int64_t bx = 2 * ps[0], by = ps[1], bz = ps[2];
     const int64_t Sx = 2 * (ps[0] + 2 * g), Sy = ps[1] + 2 * g;
     const int64_t gx = 2 * g, gy = g, gz = g;

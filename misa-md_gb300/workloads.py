@@ -15,7 +15,7 @@ run time), so the workloads are generated from a seed:
 * state: the reference's WorldBuilder lattice (src/world_builder.cpp:105-131: positions, ids 1..N
   in k, j, i scan order), random substitutional Cu/Ni from the seed, Maxwell velocities at T,
   momentum removed as WorldBuilder::zeroMomentum does (src/world_builder.cpp:143-156), then scaled
-  exactly to T as configuration::rescale does (src/system_configuration.cpp:321-346).
+  exactly to T as configuration::rescale does (src/system_configuration.cpp:86-111).
 
 Records use the reference's AtomElement layout (src/atom/atom_element.h:18-41).
 """
@@ -166,7 +166,7 @@ def write_setfl(path: str, spec: PotentialSpec) -> str:
 # slot grid
 # ----------------------------------------------------------------------------------------------
 def ghost_size(cutoff_radius_factor: float) -> int:
-    """src/simulation.cpp:120: ceil(cutoff_radius_factor) + 1 unit cells."""
+    """src/simulation.cpp:46: ceil(cutoff_radius_factor) + 1 unit cells."""
     return int(math.ceil(cutoff_radius_factor)) + 1
 
 

@@ -3,7 +3,7 @@
  *
  * C API of the CPU oracle: a single-rank restatement of MISA-MD's per-step EAM
  * hot path (src/atom.cpp, src/newton_motion.cpp, src/atom/, src/lattice/,
- * src/pack/, src/system_configuration.cpp, src/simulation.cpp:229-291).
+ * src/pack/, src/system_configuration.cpp, src/simulation.cpp:155-217).
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load
  * it, and only as the checker or the timed CPU baseline.
  *
@@ -39,7 +39,7 @@ typedef struct orc_domain_desc {
     double cutoff_radius_factor;
     int32_t grid_size[3];
     int32_t grid_coord[3];
-    int32_t ghost_size; /* <= 0: ceil(cutoff_radius_factor) + 1 as src/simulation.cpp:120 */
+    int32_t ghost_size; /* <= 0: ceil(cutoff_radius_factor) + 1 as src/simulation.cpp:46 */
 } orc_domain_desc;
 
 /* ---- Wigner-Seitz helpers on a described domain (src/lattice/ws_utils.cpp) ---- */
@@ -90,7 +90,7 @@ double orc_max_speed2(orc_sim *s);
 int64_t orc_dt_history(const orc_sim *s, double *out, int64_t cap);
 double orc_time(const orc_sim *s);
 
-/* Pieces of one step, in src/simulation.cpp:238-268 order. */
+/* Pieces of one step, in src/simulation.cpp:164-194 order. */
 void orc_firststep(orc_sim *s);
 int32_t orc_decide(orc_sim *s);
 void orc_exchange_inter(orc_sim *s);
@@ -101,11 +101,11 @@ void orc_clear_force(orc_sim *s);
 void orc_compute_eam(orc_sim *s);
 void orc_secondstep(orc_sim *s);
 
-/* prepareForStart body (src/simulation.cpp:209-219): first ghost exchange, clearForce, computeEam. */
+/* prepareForStart body (src/simulation.cpp:137-145): first ghost exchange, clearForce, computeEam. */
 void orc_prepare(orc_sim *s);
-/* nsteps of the loop body of src/simulation.cpp:238-268 (no stage hooks). */
+/* nsteps of the loop body of src/simulation.cpp:164-194 (no stage hooks). */
 void orc_simulate(orc_sim *s, int64_t nsteps);
-/* collisionStep (src/simulation.cpp:282-291). lat = (cell x, cell y, cell z, basis). */
+/* collisionStep (src/simulation.cpp:208-217). lat = (cell x, cell y, cell z, basis). */
 void orc_collision_step(orc_sim *s, const int32_t lat[4], const double dir[3], double energy_ev);
 void orc_setv(orc_sim *s, const int32_t lat[4], const double dir[3], double energy_ev);
 

@@ -1,8 +1,8 @@
 """Batched replicas (mg_batch_*): one CUDA graph advances several independent boxes.
 
-A batch runs exactly the kernels mg_simulate runs for each context, so without inter atoms (no
-floating-point atomics) a batched replica is bit-identical to the same context stepped alone; with
-cascades it follows the oracle like a single context does.
+A batch runs exactly the kernels mg_simulate runs for each context, and no kernel's result depends
+on the order in which its threads run, so a batched replica is bit-identical to the same context
+stepped alone, cascades included; cascades also follow the oracle like a single context does.
 """
 import numpy as np
 import pytest
@@ -84,6 +84,17 @@ def test_batch_cascades_follow_the_oracle(pkg, orc, wl, potentials, gpu_lib):
         assert np.abs(got["x"][loc] - want["x"][loc]).max() < 1e-9
         assert np.allclose(ctx.dt_history(), ref.dt_history(), rtol=1e-12, atol=0)
     assert min(seen) > 0
+    # the same cascades stepped alone, one context after the other: the same bits
+    for (cells, energy, seed), ctx in zip(specs, ctxs):
+        atoms = wl.build_state(cells, A0, RCF, temperature=300.0, seed=seed)
+        one = _ctx(pkg, potentials["fe"], cells, atoms, "fp64", inter_capacity=2048)
+        one.collision_step([cells[0] // 2, cells[1] // 2, cells[2] // 2, 1], wl.pka_direction(seed), energy)
+        one.set_variable_timestep(DX_MAX, DT_MIN, DT_MAX)
+        one.simulate(400)
+        (ga, ia), (gb, ib) = ctx.download(), one.download()
+        assert ga.tobytes() == gb.tobytes() and ia.tobytes() == ib.tobytes()
+        assert np.array_equal(ctx.dt_history(), one.dt_history())
+        one.close()
     batch.close()
     for c in ctxs:
         c.close()

@@ -219,6 +219,32 @@ def test_energy_parity_fp64(pkg, orc, wl, potentials, gpu_lib):
     ctx.close()
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_inter_atom_runs_are_reproducible(pkg, wl, potentials, gpu_lib, prec):
+    """Two runs of the same cascade give the same bits: the lattice atoms' shares of the inter-atom
+    pairs are summed by their owners in a fixed order, so no result depends on thread timing. After
+    the PKA and 150 steps about a dozen inter atoms remain, most of them sharing lattice neighbours;
+    dozens passed through the list on the way."""
+    cells = (10, 10, 10)
+    atoms = displaced_state(wl, cells, seed=41, n_move=80)
+    out = []
+    for _ in range(2):
+        ctx = pkg.Context(cells, A0, RCF, precision=prec, inter_capacity=4096)
+        ctx.pot_init_setfl(potentials["fecuni"] if prec == "mixed" else potentials["fe"])
+        ctx.upload(atoms)
+        ctx.prepare()
+        ctx.collision_step((5, 5, 5, 1), (0.3, 1.0, 0.2), 600.0)
+        ctx.set_variable_timestep(0.01, 1e-5, 1e-3)
+        ctx.simulate(150)
+        a, inter = ctx.download()
+        t = ctx.thermo(with_energy=True)
+        e, ei = ctx.energies(inter_cap=inter.size)
+        out.append((a.tobytes(), inter.tobytes(), e.tobytes(), ei.tobytes(), t["potential_energy"], inter.size))
+        ctx.close()
+    assert out[0] == out[1]
+    assert out[0][5] >= 8
+
+
 # ------------------------------------------------------------------------------------------------
 # migration tier: decide, exchangeInter, borderInter bit for bit
 # ------------------------------------------------------------------------------------------------
