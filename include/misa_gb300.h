@@ -355,13 +355,15 @@ mg_status mg_host_unregister(void *ptr);
  * a plugin whose host process owns all device memory, a real-time loop that must not block in the
  * allocator); mg_thermo computes the same sum but needs a context, which allocates.
  *   vx, vy, vz: device arrays of n velocities (A/ps); type: device array of n atom types
- *   (-1 vacancy, skipped; 0 Fe, 1 Cu, 2 Ni); out_mvv: device pointer to one double receiving
- *   sum m v^2 (amu A^2/ps^2); stream: a cudaStream_t (NULL for the default stream). Asynchronous.
+ *   (-1 vacancy, skipped; 0 Fe, 1 Cu, 2 Ni; the array is not validated, and any other value counts
+ *   as mass 0); out_mvv: device pointer to one double receiving sum m v^2 (amu A^2/ps^2); stream:
+ *   a cudaStream_t (NULL for the default stream). Asynchronous.
  * At most 33,554,432 atoms (MG_ERR_ARG beyond, message via mg_last_error(NULL)). The partial sums
  * live in a fixed 64 KiB __device__ array that every GPU loading the library keeps until exit and
  * that all calls on a GPU share: calls that overlap on the GPU (two streams at once) race on it.
- * The first call on each device looks up the array's address, so make that first call before any
- * stream capture begins.
+ * A call on a stream that is not being captured looks up the array's address on the current device
+ * (again after a device reset); a call on a capturing stream reuses that address, so make one call
+ * on each device before any stream capture begins (MG_ERR_STATE otherwise).
  * ------------------------------------------------------------------------------------------- */
 mg_status mg_mvv_noalloc(const double *vx, const double *vy, const double *vz, const int8_t *type, int64_t n,
                          double *out_mvv, void *stream);

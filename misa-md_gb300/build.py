@@ -17,6 +17,23 @@ LIB_PATH = os.path.join(BUILD_DIR, "libmisa_gb300.so")
 SOURCES = ["csrc/mg_kernels.cu", "csrc/mg_api.cpp", "csrc/mg_potential.cpp", "csrc/mg_noalloc.cu", "csrc/mg_world.cpp",
            "csrc/mg_dump.cpp"]
 HEADERS = ["csrc/mg_internal.h", "../include/misa_gb300.h"]
+# MISA-MD's accelerator plugin (the cuda_* hooks), built against the layout-compatible declarations in
+# arch_cuda/tree and the stand-ins in arch_cuda/config, linked to the library above
+PLUGIN_PATH = os.path.join(BUILD_DIR, "libmisa_arch_cuda.so")
+PLUGIN_SOURCES = ["arch_cuda/cuda_arch.cpp"]
+PLUGIN_HEADERS = ["../include/misa_gb300_arch.h", "arch_cuda/tree/atom/atom_element.h", "arch_cuda/tree/atom/neighbour_index.h",
+                  "arch_cuda/tree/arch/arch_imp.h", "arch_cuda/tree/arch/arch_macros.h",
+                  "arch_cuda/config/gen/arch_building_config.h", "arch_cuda/config/md_building_config.h",
+                  "arch_cuda/config/comm/domain/bcc_domain.h", "arch_cuda/config/comm/domain/domain.h",
+                  "arch_cuda/config/comm/domain/region.hpp", "arch_cuda/config/eam.h"]
+
+
+def plugin_include_flags(tree: str | None = None) -> list:
+    """Include directories of the plugin: MISA-MD's own src/ when given (tree), else the declarations in
+    arch_cuda/tree; the stand-ins for the fetched packages and CMake-written headers either way."""
+    cfg = os.path.join(HERE, "arch_cuda", "config")
+    return ["-I", tree or os.path.join(HERE, "arch_cuda", "tree"), "-I", os.path.join(cfg, "gen"), "-I", cfg,
+            "-I", os.path.join(HERE, "..", "include")]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC,-ffp-contract=off"]
 
@@ -29,10 +46,10 @@ def nvcc() -> str:
 
 
 def _stale() -> bool:
-    if not os.path.exists(LIB_PATH):
+    if not os.path.exists(LIB_PATH) or not os.path.exists(PLUGIN_PATH):
         return True
-    t = os.path.getmtime(LIB_PATH)
-    files = SOURCES + HEADERS + [os.path.relpath(__file__, HERE)]
+    t = min(os.path.getmtime(LIB_PATH), os.path.getmtime(PLUGIN_PATH))
+    files = SOURCES + HEADERS + PLUGIN_SOURCES + PLUGIN_HEADERS + [os.path.relpath(__file__, HERE)]
     return any(os.path.getmtime(os.path.join(HERE, f)) > t for f in files)
 
 
@@ -62,6 +79,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     tmp = LIB_PATH + f".tmp{os.getpid()}"
     run([cc, *NVCC_FLAGS, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread"])
     os.replace(tmp, LIB_PATH)
+    tmp = PLUGIN_PATH + f".tmp{os.getpid()}"
+    run([os.environ.get("CXX", "g++"), "-std=c++11", "-O2", "-fPIC", "-shared", "-Wall", "-Wno-non-template-friend",
+         *plugin_include_flags(), "-o", tmp, *[os.path.join(HERE, f) for f in PLUGIN_SOURCES],
+         "-L" + BUILD_DIR, "-lmisa_gb300", "-Wl,-rpath,$ORIGIN"])
+    os.replace(tmp, PLUGIN_PATH)
     return LIB_PATH
 
 

@@ -37,6 +37,7 @@ static __device__ __align__(256) double g_mvv_partials[kMaxBlocks];
 std::mutex g_setup_mutex;
 double *g_partials_addr[kMaxDevices] = {};  // device address of g_mvv_partials, per device
 
+// types other than 0, 1 and 2 weigh nothing, like vacancies (the caller's arrays are not validated)
 __device__ __forceinline__ double mass_of(int t) {  // src/types/atom_types.h:17-19
     return t == 0 ? 55.845 : (t == 1 ? 63.546 : (t == 2 ? 58.6934 : 0.0));
 }
@@ -90,11 +91,21 @@ extern "C" mg_status mg_mvv_noalloc(const double *vx, const double *vy, const do
         mg::set_global_error("mg_mvv_noalloc: no usable current device");
         return MG_ERR_CUDA;
     }
+    const cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(st, &capture);
+    if (e != cudaSuccess) {
+        mg::set_global_error(cudaGetErrorString(e));
+        return MG_ERR_CUDA;
+    }
     double *partials = nullptr;
     {
-        // first call on this device: look up the scratch array's device address (current device)
+        // Look up the scratch array's device address on the current device. Outside a capture the
+        // address is looked up again on every call, so a device reset (which reloads the module and
+        // may move the array) is picked up by the next uncaptured call; a captured call uses the
+        // address of the last uncaptured call on this device and needs one to have happened.
         std::lock_guard<std::mutex> lock(g_setup_mutex);
-        if (!g_partials_addr[dev]) {
+        if (capture == cudaStreamCaptureStatusNone) {
             double *p = nullptr;
             e = cudaGetSymbolAddress(reinterpret_cast<void **>(&p), g_mvv_partials);
             if (e != cudaSuccess || !p) {
@@ -102,15 +113,25 @@ extern "C" mg_status mg_mvv_noalloc(const double *vx, const double *vy, const do
                 return MG_ERR_CUDA;
             }
             g_partials_addr[dev] = p;
+        } else if (!g_partials_addr[dev]) {
+            mg::set_global_error("mg_mvv_noalloc: the first call on a device must come before any stream capture");
+            return MG_ERR_STATE;
         }
         partials = g_partials_addr[dev];
     }
-    const cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int64_t per_block = (int64_t) kThreads * kPerThread;
-    const int nb = static_cast<int>((n + per_block - 1) / per_block);
-    if (nb > 0) k_mvv_partial<<<nb, kThreads, 0, st>>>(vx, vy, vz, type, n, partials);
-    k_mvv_final<<<1, kThreads, 0, st>>>(partials, nb, out_mvv);
-    e = cudaGetLastError();
+    int nb = static_cast<int>((n + per_block - 1) / per_block);
+    // the launches' own return codes, so an error left by unrelated earlier work is not reported here
+    if (nb > 0) {
+        void *args[] = {&vx, &vy, &vz, &type, &n, &partials};
+        e = cudaLaunchKernel(reinterpret_cast<const void *>(k_mvv_partial), dim3(nb), dim3(kThreads), args, 0, st);
+        if (e != cudaSuccess) {
+            mg::set_global_error(cudaGetErrorString(e));
+            return MG_ERR_CUDA;
+        }
+    }
+    void *fargs[] = {&partials, &nb, &out_mvv};
+    e = cudaLaunchKernel(reinterpret_cast<const void *>(k_mvv_final), dim3(1), dim3(kThreads), fargs, 0, st);
     if (e != cudaSuccess) {
         mg::set_global_error(cudaGetErrorString(e));
         return MG_ERR_CUDA;
