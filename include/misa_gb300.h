@@ -349,6 +349,11 @@ mg_status mg_set_stage_output(mg_context *ctx, mg_dump *frames, uint64_t interva
 mg_status mg_host_register(void *ptr, uint64_t bytes);
 mg_status mg_host_unregister(void *ptr);
 
+/* Arithmetic-pipe probe (measurement; no reference counterpart): FMA throughput of the current device
+ * in FLOP/s (2 per FMA) for kind 0 FP64, 1 FP32, 2 packed FP32x2 (fma.rn.f32x2). Every SM runs
+ * independent FMA chains; one warm-up launch, then one launch timed with CUDA events. */
+mg_status mg_probe_fma(int32_t kind, double *flops_per_s);
+
 /* ---------------------------------------------------------------------------------------------
  * Sum of m v^2 over n atoms without allocating device memory. No counterpart in the reference:
  * it exists for callers that cannot call cudaMalloc (a host loop running under CUDA-graph capture,

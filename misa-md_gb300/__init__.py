@@ -116,6 +116,7 @@ _PROTOS = {
     "mg_host_register": (_I32, [_P, _U64]),
     "mg_host_unregister": (_I32, [_P]),
     "mg_mvv_noalloc": (_I32, [_P, _P, _P, _P, _I64, _P, _P]),
+    "mg_probe_fma": (_I32, [_I32, _P]),
     "mg_autotune": (_I32, [_P, _I32, _P]),
     "mg_set_tuning": (_I32, [_P, _P]),
     "mg_dump_open": (_I32, [_P, ctypes.c_char_p, _I32, _I64, _P]),
@@ -177,6 +178,16 @@ def world_build(cells, lattice_const, cutoff_radius_factor, t_set, seed, alloy_r
     if st != 0:
         raise MgError(st, (lib.mg_last_error(None) or b"").decode())
     return atoms
+
+
+def probe_fma(kind):
+    """FMA throughput of the current device in FLOP/s: kind 0 FP64, 1 FP32, 2 packed FP32x2 (mg_probe_fma)."""
+    lib = load_library()
+    out = ctypes.c_double()
+    st = lib.mg_probe_fma(int(kind), ctypes.byref(out))
+    if st != 0:
+        raise MgError(st, (lib.mg_last_error(None) or b"").decode())
+    return out.value
 
 
 def host_register(array):

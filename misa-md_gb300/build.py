@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libmisa_gb300.so")
 SOURCES = ["csrc/mg_kernels.cu", "csrc/mg_api.cpp", "csrc/mg_potential.cpp", "csrc/mg_noalloc.cu", "csrc/mg_world.cpp",
-           "csrc/mg_dump.cpp"]
+           "csrc/mg_dump.cpp", "csrc/mg_probe.cu"]
 HEADERS = ["csrc/mg_internal.h", "../include/misa_gb300.h"]
 # MISA-MD's accelerator plugin (the cuda_* hooks), built against the layout-compatible declarations in
 # arch_cuda/tree and the stand-ins in arch_cuda/config, linked to the library above

@@ -178,6 +178,11 @@ __device__ __forceinline__ f2 f2_sub(f2 a, f2 b) {
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
     return r;
 }
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b) {
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
 __device__ __forceinline__ f2 f2_mul(f2 a, f2 b) {
     f2 r;
     asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
@@ -1125,10 +1130,30 @@ __global__ void __launch_bounds__(512) k_lat_force_fp64(const __grid_constant__ 
     for (int t = t0; t < nthreads; t += gridDim.x * blockDim.x) k_lat_force_fp64_site(t, nt, g, s, in, pt, sp, kick, hook, order);
 }
 
+// Compensated force sums of the mixed form: each pair term d * fpair is added by Kahan's method
+// (W. Kahan, "Further remarks on reducing truncation errors", CACM 8(1), 1965). The running error is
+// kept negated (m = -c), so the term's product and the correction fuse into one rounding
+// (y = d * fpair + m) and a component costs four operations; x and y go through the packed f32x2
+// forms. The sum's value is s + m.
+struct ForceAcc {
+    f2 sxy, mxy;  // running sums and their negated compensations, x and y packed
+    float sz, mz;
+};
+__device__ __forceinline__ void force_acc_add(ForceAcc &a, f2 dxy, float dz, float fpair) {
+    const f2 yxy = f2_fma(dxy, f2_pack(fpair, fpair), a.mxy);
+    const f2 txy = f2_add(a.sxy, yxy);
+    a.mxy = f2_sub(yxy, f2_sub(txy, a.sxy));
+    a.sxy = txy;
+    const float yz = __fmaf_rn(dz, fpair, a.mz);
+    const float tz = __fadd_rn(a.sz, yz);
+    a.mz = __fsub_rn(yz, __fsub_rn(tz, a.sz));
+    a.sz = tz;
+}
+
 // one candidate of the force pass: the pair term when inside the cutoff (false for vacancies, NaN)
 template <int PAR>
 __device__ __forceinline__ void force_candidate(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int si,
-                                                int ti, int fbase, f2 uixy, float uiz, float dfi, int q, f2 &sxy, float &sz) {
+                                                int ti, int fbase, f2 uixy, float uiz, float dfi, int q, ForceAcc &acc) {
     const float4 D = nt.cand[PAR][q];
     const int oj = si + __float_as_int(D.w);
     const float4 uj = __ldg(s.u4 + oj);
@@ -1156,20 +1181,17 @@ __device__ __forceinline__ void force_candidate(const NeighTables &nt, const Geo
         const float phip = (zp - phi) * rinv;
         const float psip = dfi * rhojp + __ldg(s.df32 + oj) * rhoip + phip;
         const float fpair = -psip * rinv;
-        // plain FP32 accumulation: compensating it changed the force error by less than 1e-7 eV/A
-        // RMS and cost 7% of the pass
-        sxy = f2_fma(dxy, f2_pack(fpair, fpair), sxy);
-        sz = fmaf(dz, fpair, sz);
+        force_acc_add(acc, dxy, dz, fpair);
     }
 }
 template <int PAR>
 __device__ __forceinline__ void force_sum_mixed(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int si, int ti,
-                                                float4 ui, float dfi, int q0, int q1, f2 &sxy, float &sz) {
+                                                float4 ui, float dfi, int q0, int q1, ForceAcc &acc) {
     // records of the pair row ti; the table constants are read from the parameter bank where used
     const int fbase = (ti * 3) * pt.nr;
     const f2 uixy = f2_pack(ui.x, ui.y);
 #pragma unroll 1  // 2, 3, 4 and full unrolling measured slower
-    for (int q = q0; q < q1; q++) force_candidate<PAR>(nt, g, s, pt, si, ti, fbase, uixy, ui.z, dfi, q, sxy, sz);
+    for (int q = q0; q < q1; q++) force_candidate<PAR>(nt, g, s, pt, si, ti, fbase, uixy, ui.z, dfi, q, acc);
 }
 // the candidates of the warp's group list, in table order: the density pass of this step checked or
 // rebuilt the list, so it holds every pruned candidate inside the cutoff for any site of the group
@@ -1177,12 +1199,12 @@ __device__ __forceinline__ void force_sum_mixed(const NeighTables &nt, const Geo
 // loop, in the same order)
 template <int PAR>
 __device__ __forceinline__ void force_sum_listed(const NeighTables &nt, const Geom &g, const Slots &s, const PotTables &pt, int si,
-                                                 int ti, float4 ui, float dfi, const unsigned *words, f2 &sxy, float &sz) {
+                                                 int ti, float4 ui, float dfi, const unsigned *words, ForceAcc &acc) {
     const int fbase = (ti * 3) * pt.nr;
     const f2 uixy = f2_pack(ui.x, ui.y);
     for (int k = 0; k * 32 < nt.npruned; k++)
         for (unsigned w = words[k]; w; w &= w - 1)
-            force_candidate<PAR>(nt, g, s, pt, si, ti, fbase, uixy, ui.z, dfi, 32 * k + __ffs(w) - 1, sxy, sz);
+            force_candidate<PAR>(nt, g, s, pt, si, ti, fbase, uixy, ui.z, dfi, 32 * k + __ffs(w) - 1, acc);
 }
 
 // local coordinates and local index (k, j, i order) of a local slot
@@ -1213,29 +1235,30 @@ __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables 
         return;
     }
     const float dfi = s.df32[si];
-    // force sums (x and y packed, z)
-    f2 sxy = f2_pack(0.f, 0.f);
-    float sz = 0.f;
+    // compensated force sums (x and y packed, z)
+    ForceAcc acc{f2_pack(0.f, 0.f), f2_pack(0.f, 0.f), 0.f, 0.f};
     const int np = nt.npruned;
     if (lists) {
         const unsigned *w = group_list(g, s, par, u);
-        if (par) force_sum_listed<1>(nt, g, s, pt, si, ti, ui, dfi, w, sxy, sz);
-        else force_sum_listed<0>(nt, g, s, pt, si, ti, ui, dfi, w, sxy, sz);
+        if (par) force_sum_listed<1>(nt, g, s, pt, si, ti, ui, dfi, w, acc);
+        else force_sum_listed<0>(nt, g, s, pt, si, ti, ui, dfi, w, acc);
     } else {
-        if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, 0, np, sxy, sz);
-        else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, 0, np, sxy, sz);
+        if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, 0, np, acc);
+        else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, 0, np, acc);
     }
     if (in.far_flag[sl]) {
         const int nf = nt.nfull;
-        if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, np, nf, sxy, sz);
-        else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, np, nf, sxy, sz);
+        if (par) force_sum_mixed<1>(nt, g, s, pt, si, ti, ui, dfi, np, nf, acc);
+        else force_sum_mixed<0>(nt, g, s, pt, si, ti, ui, dfi, np, nf, acc);
     }
-    float sx, sy;
-    f2_unpack(sxy, sx, sy);
+    // each sum with its compensation, converted to FP64 once
+    float sx, sy, mx, my;
+    f2_unpack(acc.sxy, sx, sy);
+    f2_unpack(acc.mxy, mx, my);
     const double h = 0.5 * g.a0;
-    const double fx = h * (double) sx;
-    const double fy = h * (double) sy;
-    const double fz = h * (double) sz;
+    const double fx = h * ((double) sx + (double) mx);
+    const double fy = h * ((double) sy + (double) my);
+    const double fz = h * ((double) acc.sz + (double) acc.mz);
     const bool fused = fuse_next && kick && !hook && lattice_only(in);
     // a fused body's forces are used only in registers: the next body's firststep is taken here, and
     // the last body of a graph (never fused) stores the forces the state keeps between launches
