@@ -49,8 +49,11 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="fecuni_200c")
     p.add_argument("--fp64-steps", type=int, default=10)
-    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--cpu-seconds-small", type=float, default=8.0)
+    p.add_argument("--fe100-steps", type=int, default=1000)
+    p.add_argument("--no-small-workloads", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cells", type=int, default=0, help="override the workload's unit cells per edge")
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
@@ -167,44 +170,98 @@ class ClockSampler:
 # CPU side: the oracle (the reference's algorithm restated) timed on the host cores
 # ------------------------------------------------------------------------------------------------
 def _cpu_worker(args):
-    cells, n_ele, seed, pot_path, budget_s, cu, ni = args
+    """One oracle process: its own periodic box of `cells`, prepared, then steps until the budget is used
+    (or `steps` steps). Returns (atom-steps, seconds)."""
+    cells, seed, pot_path, budget_s, cu, ni, max_steps = args
     from oracle import oracle
+    oracle.use_timed_build()
     import __graft_entry__ as ge
     wl = ge._package().workloads
     a0, rcf = 2.855, 5.6 / 2.855
     atoms = wl.build_state(cells, a0, rcf, temperature=600.0, seed=seed, cu_frac=cu, ni_frac=ni)
     s = oracle.OracleSim(cells, a0, rcf, pot_path)
     s.set_atoms(atoms)
+    del atoms
     s.prepare()
-    s.simulate(1)
     steps, elapsed = 0, 0.0
-    while elapsed < budget_s:
+    while elapsed < budget_s and (max_steps <= 0 or steps < max_steps):
         elapsed += s.time_simulate(1)
         steps += 1
+    s.close()
     return steps * 2 * cells[0] * cells[1] * cells[2], elapsed
 
 
-def cpu_baseline(workload, pot_path, seconds):
-    """P single-threaded oracle processes (P = host cores), each stepping its own replica of a
-    bounded sub-box of the workload: the one-rank-per-core arrangement of the reference's MPI runs."""
+def rank_grid(cells, ranks):
+    """The MPI process grid that splits `cells` into `ranks` sub-boxes with the least surface (every
+    sub-box edge at least 6 cells, twice the ghost width); None when no split fits."""
+    best = None
+    for gx in range(1, ranks + 1):
+        if ranks % gx:
+            continue
+        for gy in range(1, ranks // gx + 1):
+            if (ranks // gx) % gy:
+                continue
+            gz = ranks // gx // gy
+            sub = (cells[0] // gx, cells[1] // gy, cells[2] // gz)
+            if min(sub) < 6 or any(c % g for c, g in zip(cells, (gx, gy, gz))):
+                continue
+            area = sub[0] * sub[1] + sub[1] * sub[2] + sub[0] * sub[2]
+            if best is None or area < best[0]:
+                best = (area, (gx, gy, gz), sub)
+    return None if best is None else (best[1], best[2])
+
+
+def cpu_leg(workload, pot_path, seconds, single_steps=0, single_cells=None):
+    """The reference's algorithm (the oracle, FP64, built -O3) on the host cores.
+    single: one process alone on single_cells (default: the whole box), single_steps steps or half the
+    budget. decomposed: one process per core, each stepping one sub-box of the MPI process grid that
+    splits the box over the cores, concurrently (a periodic box each: the halo exchange the MPI build
+    adds between them is not timed, so this is an upper bound on the reference's rate)."""
     from oracle import oracle
-    oracle.build()
+    oracle.build(timed=True)
     cores = os.cpu_count() or 1
-    sub = (30, 30, 30)
     ctx = mp.get_context("spawn")
-    args = [(sub, workload.n_ele, 100 + r, pot_path, seconds, workload.cu_frac, workload.ni_frac)
-            for r in range(cores)]
-    t0 = time.perf_counter()
-    with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, args)
-    wall = time.perf_counter() - t0
-    atom_steps = sum(r[0] for r in res)
-    per_proc = [r[0] / r[1] for r in res]
-    value = sum(per_proc)  # every process runs concurrently for ~seconds
-    return {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{cores} oracle processes x {sub[0]}^3-cell sub-box ({2 * sub[0]**3} atoms) of the "
-                      f"{workload.name} composition, ~{seconds:.0f} s of steps each, FP64, one thread each",
-            "wall_s": wall, "atom_steps": atom_steps}
+    w = workload
+    out = {"cores": cores, "kind": "port", "build": "g++ -O3, the compiler's default FP contraction"}
+    sc = tuple(single_cells or w.cells)
+    with ctx.Pool(1) as pool:
+        n, t = pool.map(_cpu_worker, [(sc, w.seed, pot_path, seconds / 2, w.cu_frac, w.ni_frac, single_steps)])[0]
+    out["single_thread"] = {"value": n / t, "cells": list(sc), "atoms": 2 * sc[0] * sc[1] * sc[2], "seconds": t,
+                            "atom_steps": n}
+    grid = rank_grid(w.cells, cores)
+    if grid is not None and cores > 1:
+        g, sub = grid
+        args = [(sub, w.seed + 100 + r, pot_path, seconds, w.cu_frac, w.ni_frac, 0) for r in range(cores)]
+        t0 = time.perf_counter()
+        with ctx.Pool(cores) as pool:
+            res = pool.map(_cpu_worker, args)
+        wall = time.perf_counter() - t0
+        out["decomposed"] = {"value": sum(r[0] / r[1] for r in res), "ranks": cores, "grid": list(g),
+                             "sub_box_cells": list(sub), "atoms_per_rank": 2 * sub[0] * sub[1] * sub[2],
+                             "steps_per_rank": [int(r[0] // (2 * sub[0] * sub[1] * sub[2])) for r in res],
+                             "wall_s": wall}
+    return out
+
+
+def cpu_baseline(workload, pot_path, seconds):
+    """The timed CPU baseline of the bench line: the decomposed run over all host cores (the
+    arrangement of the reference's MPI runs), with the single-thread rate of one rank's sub-box."""
+    cores = os.cpu_count() or 1
+    grid = rank_grid(workload.cells, cores)
+    sub = grid[1] if grid is not None else workload.cells
+    leg = cpu_leg(workload, pot_path, seconds, single_cells=sub)
+    if "decomposed" in leg:
+        d = leg["decomposed"]
+        value = d["value"]
+        sample = (f"{cores} oracle processes (FP64, -O3, one thread each), the {workload.name} box split as "
+                  f"{d['grid'][0]}x{d['grid'][1]}x{d['grid'][2]} MPI ranks would split it: each steps its own "
+                  f"periodic {sub[0]}x{sub[1]}x{sub[2]}-cell sub-box ({d['atoms_per_rank']} atoms) for ~{seconds:.0f} s "
+                  f"(steps {min(d['steps_per_rank'])}-{max(d['steps_per_rank'])}); no halo exchange between them")
+    else:
+        value = leg["single_thread"]["value"]
+        sample = f"one oracle process on the whole {workload.name} box for ~{seconds / 2:.0f} s"
+    return {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+            "single_thread": leg["single_thread"], "decomposed": leg.get("decomposed"), "build": leg["build"]}
 
 
 # ------------------------------------------------------------------------------------------------
@@ -222,8 +279,8 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"{w.name}: {w.n_atoms} atoms (CPU sample: {cb['sample']})"},
-            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "config": {"workload": describe(w), "cpu_sample": cb["sample"]},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "single_thread", "build")},
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -402,6 +459,54 @@ def cascade_leg(args, pkg, torch, device, tmp):
     return out
 
 
+def describe(w):
+    """The workload as the line states it, with the potential's deviations from the listed parameters."""
+    comp = "Fe" if w.n_ele == 1 else f"Fe-{w.cu_frac * 100:.1f}at%Cu-{w.ni_frac * 100:.1f}at%Ni"
+    table = ("1-element" if w.n_ele == 1 else f"{w.n_ele}-element (per-species parameters +-10% from the seed, "
+             "geometric-mean cross pairs)")
+    return (f"{w.name}: BCC {comp}, {w.cells[0]}x{w.cells[1]}x{w.cells[2]} unit cells = {w.n_atoms} atoms, periodic, "
+            f"{w.temperature:.0f} K Maxwell start, dt {w.dt * 1000:g} fs; synthetic {table} setfl, nr = nrho = 5000, "
+            f"rc 5.6 A (quintic switch from 5.0 A): Morse pair D 0.4 eV, alpha 1.4 /A, r0 2.5 A, density "
+            f"A exp(-beta (r - r0)) with beta = 1.5 /A instead of the listed 3.0 /A (with 3.0 the listed crystal is "
+            f"unstable and melts), F = -sqrt(rho), and a ZBL screened-Coulomb core below 1 A joined to the Morse "
+            f"term on [1, 2] A")
+
+
+def small_workloads_leg(args, pkg, torch, device, tmp):
+    """The 16,000-atom Fe workload (100 steps) and the 2,000,000-atom Fe workload (1000 steps) on the GPU
+    in both forms, CUDA events on the library stream, beside the oracle on the host cores."""
+    wl = pkg.workloads
+    out = {}
+    legs = (("fe_20c", 100, 100), ("fe_100c", args.fe100_steps, 2))
+    for name, steps, cpu_steps in legs:
+        w = wl.WORKLOADS[name]
+        pot = wl.workload_potential(w, tmp)
+        atoms = wl.workload_state(w)
+        rec = {"workload": describe(w), "atoms": w.n_atoms, "steps": steps}
+        for prec in ("fp64", "mixed"):
+            c = pkg.Context(w.cells, w.lattice_const, w.cutoff_radius_factor, precision=prec)
+            c.pot_init_setfl(pot)
+            c.set_timestep(w.dt)
+            c.upload(atoms)
+            c.prepare()
+            c.autotune(reps=1)
+            c.upload(atoms)   # the timed run starts from the workload's state
+            c.prepare()
+            ms = time_on_stream(torch, device, c.stream(), lambda: c.simulate(steps, sync=False))
+            c.simulate(0, sync=True)
+            rec[prec] = {"value": w.n_atoms * steps / (ms / 1e3), "ms_per_step": ms / steps}
+            c.close()
+        del atoms
+        if not args.no_cpu_baseline:
+            leg = cpu_leg(w, pot, args.cpu_seconds_small, single_steps=cpu_steps)
+            rec["cpu"] = leg
+            if cpu_steps < steps:
+                rec["cpu"]["single_thread"]["note"] = (f"{leg['single_thread']['atom_steps'] // w.n_atoms} of the "
+                                                       f"{steps} steps timed; the rate is per step")
+        out[name] = rec
+    return out
+
+
 def run_ours(args):
     rank, world, dist = dist_init(args.gpus)
     import torch
@@ -510,8 +615,11 @@ def run_ours(args):
     e2e_ctx.step_host(host, inter, n_inter, 1)  # warm
     barrier(dist, device)
     t0 = time.perf_counter()
+    e2e_ms = []
     for _ in range(args.e2e_steps):
+        tq = time.perf_counter()
         n_inter = e2e_ctx.step_host(host, inter, n_inter, 1)
+        e2e_ms.append((time.perf_counter() - tq) * 1e3)
     e2e_value, e2e_s = whole_job_rate(dist, device, n_atoms * args.e2e_steps, time.perf_counter() - t0)
     pkg.host_unregister(host)
     e2e_ctx.close()
@@ -542,6 +650,14 @@ def run_ours(args):
         except Exception as exc:
             cascades = {"error": f"{type(exc).__name__}: {exc}"}
 
+    small = None
+    if world == 1 and not args.no_small_workloads:
+        try:
+            small = small_workloads_leg(args, pkg, torch, device, tmp)
+        except Exception as exc:
+            small = {"error": f"{type(exc).__name__}: {exc}"}
+    pipes = {k: pkg.probe_fma(i) / 1e12 for i, k in enumerate(("fp64_tflops", "fp32_tflops", "fp32x2_tflops"))}
+
     cb = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(w, pot, args.cpu_seconds)
@@ -559,18 +675,17 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
-        "dtype_detail": "f32 distances, spline lookups and pair terms; Kahan-compensated f32 density sums, f32 "
-                        "force sums; f64 positions, "
-                        "velocities, Verlet and reductions", "data": "synthetic",
-        "config": {"workload": f"{w.name}: BCC Fe-1.5at%Cu-1.0at%Ni, {w.cells[0]}^3 unit cells = {n_atoms} atoms, "
-                               f"{w.temperature:.0f} K Maxwell start, dt {w.dt * 1000:.0f} fs, synthetic 3-element setfl "
-                               f"(nr = nrho = 5000, rc 5.6 A)",
+        "dtype_detail": "f32 distances, spline lookups and pair terms; Kahan-compensated f32 density and force sums, "
+                        "each converted to f64 once per atom; f64 positions, velocities, Verlet and reductions",
+        "data": "synthetic",
+        "config": {"workload": describe(w),
                    "precision": "mixed", "l2": "working set ~1.9 GB > 129 MB L2 (no flush needed)",
                    "timing": "value: CUDA-graph replay (16 loop bodies per launch, each force pass but the last taking "
                              "the next body's firststep) timed with CUDA events on the library stream; kernel times: "
                              "a second pass of the same steps with events around every kernel",
                    "parallelism": f"{world} independent replica(s), one per GPU"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io,
+                "ms_per_step": [round(t, 2) for t in e2e_ms], "median_ms_per_step": statistics.median(e2e_ms),
                 "path": "mg_step_host: pinned host slot array in, one loop body, slot array out; copies in 16 z-slabs "
                         "overlapped with unpack/firststep (in) and the force pass (out)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
@@ -587,13 +702,15 @@ def run_ours(args):
         "accuracy": {"force_rms_ev_per_A": f_rms, "force_max_ev_per_A": f_max, "reference": "FP64 GPU form",
                      "nve_drift": drift},
         "cascades": cascades,
+        "workloads": small,
+        "pipes": dict(pipes, source="mg_probe_fma: independent FMA chains on every SM, CUDA events"),
         "gpu_launches": launches,
         "tuning": tuning,
         "clocks": clocks,
         "state": {"n_inter": thermo["n_inter"], "device_errors": thermo["device_errors"], "gen_s": gen_s},
     }
     if cb is not None:
-        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "single_thread", "build")}
     print(json.dumps(line))
 
 

@@ -14,6 +14,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+# the same source built with the compiler's default FP contraction, for the timed CPU baseline only
+TIMED_LIB_PATH = os.path.join(HERE, "_build", "liboracle_timed.so")
 
 ATOM_DTYPE = np.dtype(
     [("id", "<u8"), ("type", "<i4"), ("pad_", "<i4"), ("x", "<f8", (3,)), ("v", "<f8", (3,)),
@@ -77,12 +79,22 @@ class DomainDesc(ctypes.Structure):
                 ("grid_coord", ctypes.c_int32 * 3), ("ghost_size", ctypes.c_int32)]
 
 
-def build(force=False):
+def build(force=False, timed=False):
+    path = TIMED_LIB_PATH if timed else LIB_PATH
     src = os.path.join(HERE, "misa_oracle.cpp")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(src) > os.path.getmtime(LIB_PATH) or \
-            os.path.getmtime(os.path.join(HERE, "misa_oracle.h")) > os.path.getmtime(LIB_PATH):
-        subprocess.run(["make", "-s", "-C", HERE, "-B" if force else "_build/liboracle.so"], check=True)
-    return LIB_PATH
+    if force or not os.path.exists(path) or os.path.getmtime(src) > os.path.getmtime(path) or \
+            os.path.getmtime(os.path.join(HERE, "misa_oracle.h")) > os.path.getmtime(path):
+        target = os.path.relpath(path, HERE)
+        subprocess.run(["make", "-s", "-C", HERE] + (["-B"] if force else []) + [target], check=True)
+    return path
+
+
+def use_timed_build():
+    """Make this process load the timed build (the CPU baseline's workers call it before lib())."""
+    global LIB_PATH
+    if _LIB is not None:
+        raise RuntimeError("the oracle library is already loaded")
+    LIB_PATH = TIMED_LIB_PATH
 
 
 _LIB = None
