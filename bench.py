@@ -464,9 +464,11 @@ def describe(w):
     comp = "Fe" if w.n_ele == 1 else f"Fe-{w.cu_frac * 100:.1f}at%Cu-{w.ni_frac * 100:.1f}at%Ni"
     table = ("1-element" if w.n_ele == 1 else f"{w.n_ele}-element (per-species parameters +-10% from the seed, "
              "geometric-mean cross pairs)")
+    r0 = ("r0 2.65 A instead of the listed 2.5 A (with 2.5 the single-element BCC crystal transforms within "
+          "0.5 ps)" if w.n_ele == 1 else "r0 2.5 A")
     return (f"{w.name}: BCC {comp}, {w.cells[0]}x{w.cells[1]}x{w.cells[2]} unit cells = {w.n_atoms} atoms, periodic, "
             f"{w.temperature:.0f} K Maxwell start, dt {w.dt * 1000:g} fs; synthetic {table} setfl, nr = nrho = 5000, "
-            f"rc 5.6 A (quintic switch from 5.0 A): Morse pair D 0.4 eV, alpha 1.4 /A, r0 2.5 A, density "
+            f"rc 5.6 A (quintic switch from 5.0 A): Morse pair D 0.4 eV, alpha 1.4 /A, {r0}, density "
             f"A exp(-beta (r - r0)) with beta = 1.5 /A instead of the listed 3.0 /A (with 3.0 the listed crystal is "
             f"unstable and melts), F = -sqrt(rho), and a ZBL screened-Coulomb core below 1 A joined to the Morse "
             f"term on [1, 2] A")

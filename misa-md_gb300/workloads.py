@@ -52,6 +52,16 @@ class EamParams:
     beta: float = 1.5
 
 
+# Morse minimum and density reference distance of the single-element table. The listed 2.5 A gives a
+# BCC crystal at a0 = 2.855 A that is unstable along the Bain path (its energy falls toward c/a < 1),
+# and a 600 K box transforms after ~0.4 ps (inter atoms grow to a quarter of all atoms by 1 ps).
+# With 2.65 A the BCC site is a minimum along the Bain path, the Einstein constant rises from 3.2 to
+# 6.5 eV/A^2, and 64k- and 2M-atom boxes at 300 K and 600 K stay on their lattice through 3000 steps.
+# The multi-element tables keep the listed 2.5 A as the centre of their per-species perturbations:
+# the dilute Fe-Cu-Ni alloy built from it is stable as listed.
+SINGLE_ELEMENT_R0 = 2.65
+
+
 @dataclass
 class PotentialSpec:
     n_ele: int = 1
@@ -71,7 +81,7 @@ class PotentialSpec:
         if not self.params:
             base = EamParams()
             if self.n_ele == 1:
-                self.params = [base]
+                self.params = [EamParams(r0=SINGLE_ELEMENT_R0)]
             else:
                 rng = np.random.default_rng(self.seed)
                 self.params = []
