@@ -589,25 +589,6 @@ def run_ours(args):
                               "tuning": tuning}))
         return
 
-    # ---- accuracy of the mixed form against the FP64 form on the same state ----
-    ctx64 = make_ctx("fp64")
-    a64, _ = ctx64.download()
-    ctxm = make_ctx("mixed")
-    am, _ = ctxm.download()
-    ctxm.close()
-    loc = wl.local_slot_indices(w.cells, w.cutoff_radius_factor)
-    d = am["f"][loc] - a64["f"][loc]
-    f_rms = float(np.sqrt((d ** 2).mean()))
-    f_max = float(np.abs(d).max())
-    del a64, am, d
-
-    # ---- plain FP64, resident ----
-    ctx64.simulate(2, sync=True)
-    ms64 = time_on_stream(torch, device, ctx64.stream(), lambda: ctx64.simulate(args.fp64_steps, sync=False))
-    value64, s64 = whole_job_rate(dist, device, n_atoms * args.fp64_steps, ms64 / 1e3)
-    ms64 = s64 * 1e3 / args.fp64_steps
-    ctx64.close()
-
     # ---- end to end through the drop-in call (host slot array, pinned) ----
     host = atoms.copy()
     inter = np.zeros(ctx.n_slots // 100 + 1024, dtype=pkg.ATOM_DTYPE)
@@ -627,6 +608,25 @@ def run_ours(args):
     e2e_ctx.close()
     bytes_io = host.nbytes + n_inter * pkg.ATOM_DTYPE.itemsize
     del host
+    # ---- accuracy of the mixed form against the FP64 form on the same state ----
+    ctx64 = make_ctx("fp64")
+    a64, _ = ctx64.download()
+    ctxm = make_ctx("mixed")
+    am, _ = ctxm.download()
+    ctxm.close()
+    loc = wl.local_slot_indices(w.cells, w.cutoff_radius_factor)
+    d = am["f"][loc] - a64["f"][loc]
+    f_rms = float(np.sqrt((d ** 2).mean()))
+    f_max = float(np.abs(d).max())
+    del a64, am, d
+
+    # ---- plain FP64, resident ----
+    ctx64.simulate(2, sync=True)
+    ms64 = time_on_stream(torch, device, ctx64.stream(), lambda: ctx64.simulate(args.fp64_steps, sync=False))
+    value64, s64 = whole_job_rate(dist, device, n_atoms * args.fp64_steps, ms64 / 1e3)
+    ms64 = s64 * 1e3 / args.fp64_steps
+    ctx64.close()
+
     ctx.close()
     del atoms
 
