@@ -435,6 +435,23 @@ def cascade_leg(args, pkg, torch, device, tmp):
         s64 += time.perf_counter() - t0
         atoms64 += atoms_r[r]
         c.close()
+    # one whole FP64 cascade of the median-size replica, against its own window-based estimate
+    rm = int(order[len(order) // 2])
+    sp = specs[rm]
+    c = cascade_ctx(pkg, sp["cells"], a0, rcf, pot4, states[rm], "fp64", sp["lat"], sp["dir"], sp["energy"])
+    c.simulate(3, sync=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    c.simulate(win, sync=True)
+    s_win = time.perf_counter() - t0
+    c.close()
+    c = cascade_ctx(pkg, sp["cells"], a0, rcf, pot4, states[rm], "fp64", sp["lat"], sp["dir"], sp["energy"])
+    c.simulate(3, sync=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    c.simulate(cs.steps, sync=True)
+    s_whole = time.perf_counter() - t0
+    c.close()
     del states
     seq64_full_s = s64 / atoms64 * atoms_r.sum() * (cs.steps / win)
     batched_s = ms_b / 1e3
@@ -448,6 +465,9 @@ def cascade_leg(args, pkg, torch, device, tmp):
         "cascades_per_hour_sequential_fp64": cs.replicas * 3600.0 / seq64_full_s,
         "batched_mixed_over_sequential_fp64": seq64_full_s / batched_s,
         "sequential_fp64_sample": f"{len(pick)} replicas (size-stratified) x {win} steps, scaled by atoms and steps",
+        "fp64_whole_cascade": {"replica_cells": sp["cells"], "atoms": int(atoms_r[rm]), "steps": cs.steps,
+                               "measured_s": s_whole, "window_estimate_s": s_win * cs.steps / win,
+                               "measured_over_estimate": s_whole / (s_win * cs.steps / win)},
         "window": {"steps": win, "batched_mixed_s": ms_bw / 1e3, "sequential_mixed_s": s_sw,
                    "batching_gain": s_sw / (ms_bw / 1e3)},
         "graph_steps_per_launch": args.cascade_graph_steps,
