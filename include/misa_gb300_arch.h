@@ -8,6 +8,9 @@
  * of misa_gb300.h; the hooks return void and, like the reference's own failures, a failed call ends the
  * process (the library's message goes to stderr). C++ linkage, as the reference declares them.
  *
+ * The hooks keep one context per process (the reference calls them from its single rank thread); they
+ * are not thread-safe.
+ *
  * Settings the arguments do not carry are read from the environment at cuda_env_init:
  * MISA_GB300_DEVICE (default 0), MISA_GB300_PRECISION ("fp64", default, or "mixed") and
  * MISA_GB300_SETFL (the setfl file the run's potential came from; pot v0.1.0's eam class has no
@@ -24,7 +27,7 @@ class BccDomain;                    /* libcomm v0.3.3's domain: phase_space, sub
                                        lattice_const, cutoff_radius_factor are read */
 }
 template <class T>
-class NeighbourIndex;               /* src/atom/neighbour_index.h:16-110, read as a friend */
+class NeighbourIndex;               /* src/atom/neighbour_index.h:16-77, read as a friend */
 
 /* archEnvInit / archEnvFinalize (src/arch/arch_env.hpp:15-25): device selection, context teardown. */
 void cuda_env_init();

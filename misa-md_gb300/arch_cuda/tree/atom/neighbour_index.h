@@ -1,4 +1,4 @@
-// MISA-MD's neighbour offset tables (src/atom/neighbour_index.h:16-110), declared here for builds
+// MISA-MD's neighbour offset tables (src/atom/neighbour_index.h:16-77), declared here for builds
 // without the MISA-MD tree: the class template, its four protected tables and the friend declaration
 // through which the plugin's cuda_nei_offset_init reads them. The reference fills the tables in make();
 // here they are given to the constructor, which is all a host without the tree can do.
