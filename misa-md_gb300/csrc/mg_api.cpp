@@ -870,6 +870,7 @@ mg_status mg_set_variable_timestep(mg_context *ctx, double dx_max, double dt_min
         return MG_ERR_ARG;
     }
     set_dt(ctx, dt_max, dx_max, dt_min, dt_max);
+    ctx->vmax_stale = true;  // the fixed-dt kicks before this did not keep the max-|v| words
     return check_launch(ctx);
 }
 

@@ -203,6 +203,9 @@ __device__ __forceinline__ double speed2(double vx, double vy, double vz) {
 // Max of v2 over the lanes that call this together, then one atomicMax per such group into a word
 // picked by the warp's index, so the words see few atomics each. Non-negative doubles order like
 // their bit patterns, so the max is taken on the 64-bit patterns, high word first.
+// The max-|v|^2 words feed only the variable-timestep rule; the kicks of a fixed-dt run skip them, and
+// the host recomputes them (k_vmax_full) before the first step after the rule is switched on.
+__device__ __forceinline__ bool variable_dt(const StepParams *sp) { return sp->dx_max > 0.0; }
 __device__ __forceinline__ void note_vmax2(StepParams *sp, double v2) {
     const unsigned mask = __activemask();
     const unsigned long long b = (unsigned long long) __double_as_longlong(v2);
@@ -1115,7 +1118,7 @@ __device__ __forceinline__ void k_lat_force_fp64_site(int t, const NeighTables &
         const double vy = __dadd_rn(s.vy[sl], __dmul_rn(c, fy));
         const double vz = __dadd_rn(s.vz[sl], __dmul_rn(c, fz));
         s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz;
-        note_vmax2(sp, speed2(vx, vy, vz));
+        if (variable_dt(sp)) note_vmax2(sp, speed2(vx, vy, vz));
     }
 }
 template <bool LOOP>  // LOOP: several sites per thread, one grid stride apart
@@ -1269,7 +1272,7 @@ __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables 
         const double vy = __dadd_rn(s.vy[sl], __dmul_rn(c, fy));
         const double vz = __dadd_rn(s.vz[sl], __dmul_rn(c, fz));
         if (!fuse_next) { s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz; }  // else first_half writes the next v
-        note_vmax2(sp, speed2(vx, vy, vz));
+        if (variable_dt(sp)) note_vmax2(sp, speed2(vx, vy, vz));
         if (fuse_next) {
             // the next loop body's firststep for this atom, with the force still in registers (the
             // other threads of this pass still read this atom's u4, so the new record goes to the next
