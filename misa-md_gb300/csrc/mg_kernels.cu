@@ -200,12 +200,12 @@ __device__ __forceinline__ double dt_inv_m_of(const StepParams *p, int type) {
 __device__ __forceinline__ double speed2(double vx, double vy, double vz) {
     return __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz));
 }
-// Max of v2 over the lanes that call this together, then one atomicMax per such group into a word
-// picked by the warp's index, so the words see few atomics each. Non-negative doubles order like
-// their bit patterns, so the max is taken on the 64-bit patterns, high word first.
 // The max-|v|^2 words feed only the variable-timestep rule; the kicks of a fixed-dt run skip them, and
 // the host recomputes them (k_vmax_full) before the first step after the rule is switched on.
 __device__ __forceinline__ bool variable_dt(const StepParams *sp) { return sp->dx_max > 0.0; }
+// Max of v2 over the lanes that call this together, then one atomicMax per such group into a word
+// picked by the warp's index, so the words see few atomics each. Non-negative doubles order like
+// their bit patterns, so the max is taken on the 64-bit patterns, high word first.
 __device__ __forceinline__ void note_vmax2(StepParams *sp, double v2) {
     const unsigned mask = __activemask();
     const unsigned long long b = (unsigned long long) __double_as_longlong(v2);
