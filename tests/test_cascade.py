@@ -89,6 +89,33 @@ def test_variable_timestep_clock_and_history(pkg, orc, wl, potentials, gpu_lib):
     ctx.close()
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_variable_timestep_after_fixed_steps(pkg, wl, potentials, gpu_lib, prec):
+    """Fixed-dt kicks leave the max-|v| words alone; switching the variable rule on (with no other call
+    in between) must still give the rule applied to the current velocities, bit for bit. The mixed
+    form runs the 20 fixed steps as a fused graph of 16 bodies and 4 single bodies."""
+    cells = (8, 8, 8)
+    atoms = wl.build_state(cells, A0, RCF, temperature=900.0, seed=63)
+    ctx = pkg.Context(cells, A0, RCF, precision=prec)
+    ctx.pot_init_setfl(potentials["fe"])
+    ctx.upload(atoms)
+    ctx.prepare()
+    ctx.set_timestep(0.001)
+    ctx.simulate(20)
+    ctx.set_variable_timestep(DX_MAX, DT_MIN, DT_MAX)
+    loc = wl.local_slot_indices(cells, RCF)
+    want = []
+    for _ in range(4):
+        got_atoms, inter = ctx.download()
+        want.append(_rule(_speed2_max(got_atoms, loc, inter)))
+        ctx.simulate(1)
+    hist = ctx.dt_history()
+    assert np.array_equal(hist[:20], [0.001] * 20)
+    assert np.array_equal(hist[20:], want)
+    ctx.close()
+
+
 def _cascade_pair(pkg, orc, wl, pot, cells, seed, energy, precision):
     atoms = wl.build_state(cells, A0, RCF, temperature=300.0, seed=seed)
     ctx = pkg.Context(cells, A0, RCF, precision=precision, inter_capacity=4096)

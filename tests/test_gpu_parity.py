@@ -463,3 +463,14 @@ def test_contexts_with_different_boxes_coexist(pkg, orc, wl, potentials, gpu_lib
         loc = local(wl, cells)
         assert np.abs(got["f"][loc] - want["f"][loc]).max() < F64_TOL
         ctx.close()
+
+
+def test_fma_probe_orders_the_pipes(pkg, gpu_lib):
+    """mg_probe_fma: FP64, FP32 and packed FP32x2 FMA throughput of this GPU, in FLOP/s. On GB300 the
+    FP64 pipe is tens of times slower than FP32, and the packed form is at least as fast as scalar FP32."""
+    f64, f32, f32x2 = (pkg.probe_fma(k) for k in range(3))
+    assert 0.1e12 < f64 < 10e12
+    assert f32 > 20 * f64
+    assert f32x2 > 0.9 * f32
+    with pytest.raises(pkg.MgError):
+        pkg.probe_fma(3)
