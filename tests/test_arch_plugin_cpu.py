@@ -45,3 +45,36 @@ def test_plugin_compiles_against_the_reference_headers(pkg, tmp_path):
     sys.path.insert(0, os.path.join(HERE, "golden"))
     import make_hook_symbols
     assert make_hook_symbols.reference_symbols(REFERENCE_SRC) == golden()
+
+
+def test_plugin_failure_ends_the_process_with_the_message(pkg, tmp_path):
+    """The hooks return void and MISA-MD has no error channel for them, so a failed call prints the
+    library's message and aborts, as the reference's own failures end the job. Here cuda_domain_init
+    gets a domain split over two ranks along x, which the plugin (one box on one GPU) rejects before
+    touching a device, so the check runs the same with or without a GPU."""
+    import signal
+    pkg.build.build()
+    names = golden()
+    dom = next(n for n, d in names.items() if d.startswith("cuda_domain_init"))
+    code = f'''
+import ctypes, os, sys
+lib = ctypes.CDLL({pkg.build.PLUGIN_PATH!r})
+sup = ctypes.CDLL(sys.argv[1])
+sup.th_domain_new.restype = ctypes.c_void_p
+sup.th_domain_new.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int32]
+import numpy as np
+cells = np.array([8, 8, 8], dtype=np.int64)
+d = sup.th_domain_new(cells.ctypes.data, 2.855, 5.6 / 2.855, 2)
+# a domain split over two ranks along x: the plugin runs one box on one GPU
+ctypes.c_int64.from_address(d + 3 * 8).value = 4
+getattr(lib, {dom!r}).argtypes = [ctypes.c_void_p]
+getattr(lib, {dom!r})(d)
+print("returned")
+'''
+    support = str(tmp_path / "libhooks_support.so")
+    subprocess.run(["g++", "-std=c++11", "-O1", "-fPIC", "-shared", "-w", *pkg.build.plugin_include_flags(), "-o", support,
+                    os.path.join(HERE, "arch_hooks_support.cpp")], check=True)
+    r = subprocess.run([sys.executable, "-c", code, support], capture_output=True, text=True, timeout=120)
+    assert r.returncode == -signal.SIGABRT, (r.returncode, r.stdout, r.stderr)
+    assert "returned" not in r.stdout
+    assert "misa_gb300 cuda_domain_init failed" in r.stderr
