@@ -590,11 +590,12 @@ def run_ours(args):
     gc.collect()
     gc.disable()
     t0 = time.perf_counter()
-    e2e_ms = []
+    e2e_ms, e2e_inter = [], []
     for _ in range(args.e2e_steps):
         tq = time.perf_counter()
         n_inter = e2e_ctx.step_host(host, inter, n_inter, 1)
         e2e_ms.append((time.perf_counter() - tq) * 1e3)
+        e2e_inter.append(int(n_inter))
     e2e_value, e2e_s = whole_job_rate(dist, device, n_atoms * args.e2e_steps, time.perf_counter() - t0)
     gc.enable()
     pkg.host_unregister(host)
@@ -715,6 +716,7 @@ def run_ours(args):
                    "parallelism": f"{world} independent replica(s), one per GPU"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io,
                 "ms_per_step": [round(t, 2) for t in e2e_ms], "median_ms_per_step": statistics.median(e2e_ms),
+                "inter_atoms_per_step": e2e_inter,
                 "path": "mg_step_host: pinned host slot array in, one loop body, slot array out; copies in 16 z-slabs "
                         "overlapped with unpack/firststep (in) and the force pass (out)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
