@@ -1926,11 +1926,14 @@ __device__ __forceinline__ double lat_df(const Geom &g, const Slots &s, int sl, 
 }
 
 // kind: 0 density, 1 force, 2 energy
-// One warp per inter atom (the lists hold a few to thousands of atoms, each with ~460 partner
-// entries): the lanes share the 229 lattice entries and the 229 bucket keys of the atom's nearest
-// site, keep partial sums, and reduce them by shuffles in a fixed order. Every lattice owner with a
-// partner inside the cutoff is listed once (touch_owner) for k_inter_owner, which adds the owner's
-// share of the pair terms.
+// One block of kInterThreads per inter atom (the lists hold a few to thousands of atoms, each with
+// ~460 partner entries): the threads share the 229 lattice entries and the 229 bucket keys of the
+// atom's nearest site, two each, keep partial sums, and reduce them in a fixed order (shuffles within
+// a warp, then the warps in order). With a few inter atoms the pass is one chain of dependent FP64
+// spline evaluations per thread, so spreading an atom over four warps instead of one cuts its
+// latency. Every lattice owner with a partner inside the cutoff is listed once (touch_owner) for
+// k_inter_owner, which adds the owner's share of the pair terms.
+constexpr int kInterThreads = 128;
 __device__ __forceinline__ double warp_sum_d(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
@@ -1949,12 +1952,12 @@ __device__ __forceinline__ bool is_local_slot(const Geom &g, int sl) {
     return X >= g.gx && X < g.gx + g.bx && Y >= g.gy && Y < g.gy + g.by && Z >= g.gz && Z < g.gz + g.bz;
 }
 template <int KIND>
-__global__ void __launch_bounds__(128) k_inter_eam(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool mixed) {
+__global__ void __launch_bounds__(kInterThreads) k_inter_eam(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool mixed) {
     const int n = in.cnt[CNT_INTER];
     const int nb = *in.n_bucket;
-    const int lane = threadIdx.x & 31;
-    const int warps = gridDim.x * (blockDim.x >> 5);
-    for (int a = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); a < n; a += warps) {  // warp-uniform
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ double red[3][kInterThreads / 32];
+    for (int a = blockIdx.x; a < n; a += gridDim.x) {  // block-uniform
         const double xa = in.x[a], ya = in.y[a], za = in.z[a];
         const int ta = in.type[a];
         const uint64_t ida = in.id[a];
@@ -1965,7 +1968,7 @@ __global__ void __launch_bounds__(128) k_inter_eam(const __grid_constant__ Neigh
         // lattice partners: the nearest site's atom, then the full offsets of that site
         const int par = (near % g.Sx) & 1;
         const int nf = nt.nfull;
-        for (int q = lane - 1; q < nf; q += 32) {
+        for (int q = (int) threadIdx.x - 1; q < nf; q += kInterThreads) {
             const int sj = q < 0 ? near : near + (par ? nt.full[1][q] : nt.full[0][q]);
             if (sj < 0 || sj >= g.n_slots) { set_error(in, MG_DEVERR_OUT_OF_GRID); continue; }
             const int tj = s.type[sj];
@@ -1984,7 +1987,7 @@ __global__ void __launch_bounds__(128) k_inter_eam(const __grid_constant__ Neigh
             }
         }
         // inter partners: same-site bucket (not itself), then the buckets of the full offsets
-        for (int q = lane - 1; q < nf; q += 32) {
+        for (int q = (int) threadIdx.x - 1; q < nf; q += kInterThreads) {
             const int key = q < 0 ? near : near + (par ? nt.full[1][q] : nt.full[0][q]);
             for (int b = bucket_begin(in, nb, key); b < nb && (int) (in.bucket[b] >> 32) == key; b++) {
                 const InterRef o = inter_ref(in, (int) (in.bucket[b] & 0xffffffffLL));
@@ -2001,14 +2004,27 @@ __global__ void __launch_bounds__(128) k_inter_eam(const __grid_constant__ Neigh
                 }
             }
         }
+        // the threads' partial sums: shuffles within each warp, then the warps' sums in warp order
         if (KIND == 1) {
             fx = warp_sum_d(fx);
             fy = warp_sum_d(fy);
             fz = warp_sum_d(fz);
+            if (lane == 0) { red[0][warp] = fx; red[1][warp] = fy; red[2][warp] = fz; }
         } else {
             acc = warp_sum_d(acc);
+            if (lane == 0) red[0][warp] = acc;
         }
-        if (lane != 0) continue;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            acc = red[0][0]; fy = red[1][0]; fz = red[2][0];
+            for (int w = 1; w < kInterThreads / 32; w++) {
+                acc += red[0][w];
+                if (KIND == 1) { fy += red[1][w]; fz += red[2][w]; }
+            }
+            fx = acc;
+        }
+        __syncthreads();  // red is reused by the block's next atom
+        if (threadIdx.x != 0) continue;
         if (KIND == 0) {
             in.rho[a] = acc;
             int m; double p;
@@ -2096,7 +2112,7 @@ __global__ void __launch_bounds__(128) k_inter_owner(const __grid_constant__ Nei
 }
 template <int KIND>
 void launch_inter_kind(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
-    k_inter_eam<KIND><<<lc.num_sms * 4, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
+    k_inter_eam<KIND><<<lc.num_sms * 4, kInterThreads, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
     k_inter_owner<KIND><<<lc.num_sms * 4, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
 }
 void launch_inter_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
