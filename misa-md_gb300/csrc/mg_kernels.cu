@@ -1645,6 +1645,19 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
     __shared__ int sh_n;
     const int tid = threadIdx.x, nthr = blockDim.x;
 
+    // The usual step of a crystal: no inter atom, no ghost image and nothing displaced, so every
+    // phase would find its lists empty; what remains is decide voiding the previous step's far list
+    // and the index being empty. The counts are read by all threads before any is written.
+    const bool idle = in.cnt[CNT_INTER] == 0 && in.cnt[CNT_GHOST] == 0 && in.cnt[CNT_DISPLACED] == 0;
+    __syncthreads();
+    if (idle) {
+        if (tid == 0) {
+            if (mask & MANAGE_DECIDE) in.cnt[CNT_FAR] = 0;
+            if (mask & MANAGE_INDEX) *in.n_bucket = 0;
+        }
+        return;
+    }
+
     if (mask & MANAGE_CLEAR_GHOST) {
         if (tid == 0) in.cnt[CNT_GHOST] = 0;
         __syncthreads();
