@@ -1044,7 +1044,7 @@ __global__ void k_lat_df(Geom g, Slots s, Inter in, PotTables pt, bool hook) {
 }
 void launch_lat_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook) {
     const int b = 256;
-    const int n = hook ? (g.n_local + b - 1) / b : lc.num_sms * 8;
+    const int n = hook ? (g.n_local + b - 1) / b : std::max(1, std::min(lc.num_sms * 8, (g.n_local + b - 1) / b));
     if (mixed) k_lat_df<true><<<n, b, 0, lc.stream>>>(g, s, in, t, hook);
     else k_lat_df<false><<<n, b, 0, lc.stream>>>(g, s, in, t, hook);
 }
@@ -1357,8 +1357,13 @@ __global__ void k_secondstep(Geom g, Slots s, Inter in, StepParams *p, int latti
     }
     if (v2max > 0.0) note_vmax2(p, v2max);
 }
+// grid-stride kernels that often have nothing to do: a grid no larger than the box needs, so a
+// small box does not schedule a thousand idle blocks every step
+inline int box_grid(const LaunchCtx &lc, const Geom &g, int per_sm, int threads) {
+    return std::max(1, std::min(lc.num_sms * per_sm, (g.n_local + threads - 1) / threads));
+}
 void launch_secondstep(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, StepParams *p, bool lattice) {
-    k_secondstep<<<lc.num_sms * 8, 256, 0, lc.stream>>>(g, s, in, p, lattice ? 1 : 2);
+    k_secondstep<<<box_grid(lc, g, 8, 256), 256, 0, lc.stream>>>(g, s, in, p, lattice ? 1 : 2);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -2065,6 +2070,7 @@ __global__ void __launch_bounds__(kInterThreads) k_inter_eam(const __grid_consta
 template <int KIND>
 __global__ void __launch_bounds__(128) k_inter_owner(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool mixed) {
     const int n = min(in.cnt[CNT_TOUCHED], in.tcap);
+    if (n == 0) return;  // nothing listed: no block writes, so no reset is due
     const int nb = *in.n_bucket;
     const int lane = threadIdx.x & 31;
     const int warps = gridDim.x * (blockDim.x >> 5);
