@@ -217,7 +217,7 @@ void seq_eam_rho(mg_context *ctx, Timer *t) {
 // the inter-atom force pass and the second half-kick, after the lattice force pass
 void seq_eam_force_tail(mg_context *ctx, bool kick, Timer *t) {
     const LaunchCtx lc = ctx->lc();
-    launch_inter_force(lc, ctx->g, ctx->s, ctx->in, ctx->pt, ctx->mixed());
+    launch_inter_force(lc, ctx->g, ctx->s, ctx->in, ctx->pt, ctx->mixed(), ctx->d_sp, kick);
     if (t) t->mark(10);
     if (kick) launch_secondstep(lc, ctx->g, ctx->s, ctx->in, ctx->d_sp, false);
     if (t) t->mark(11);

@@ -314,7 +314,10 @@ void launch_far_rebuild(const LaunchCtx &lc, const Geom &g, Slots s, Inter in);
 void launch_inter_manage(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, int steps_mask, bool mixed);
 enum { MANAGE_DECIDE = 1, MANAGE_CLEAR_GHOST = 2, MANAGE_EXCHANGE = 4, MANAGE_BORDER = 8, MANAGE_INDEX = 16 };
 void launch_inter_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed);
-void launch_inter_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed);
+// kick: the second half-kick of the lattice owners the density pass's inter-atom sweep listed (the
+// lattice force pass kicked every other atom)
+void launch_inter_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, StepParams *sp,
+                        bool kick);
 void launch_inter_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed);
 void launch_inter_firststep(const LaunchCtx &lc, Inter in, const StepParams *sp);
 void launch_setv(const LaunchCtx &lc, const Geom &g, Slots s, int64_t slot, const double dir[3], double energy);

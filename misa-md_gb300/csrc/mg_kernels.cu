@@ -221,6 +221,13 @@ __device__ __forceinline__ void set_error(Inter &in, uint32_t bit) { atomicOr((u
 // Lattice passes can fuse df / the half-kick only when no other kernel adds density or force to
 // lattice slots afterwards, i.e. when there are no inter atoms.
 __device__ __forceinline__ bool lattice_only(const Inter &in) { return in.cnt[CNT_INTER] == 0; }
+// Whether the lattice force pass may take the second half-kick of slot sl itself: always without inter
+// atoms; with them, for every atom the density pass's inter-atom sweep did not list (no inter atom
+// within the cutoff, so no inter-atom force is added later). The listed owners are kicked by the
+// inter-atom force pass's owner gather once their force is complete.
+__device__ __forceinline__ bool kick_in_lattice_pass(const Inter &in, int sl) {
+    return lattice_only(in) || !((in.touch_bits[sl >> 5] >> (sl & 31)) & 1u);
+}
 // FP64 displacement test of atom::decide (src/atom.cpp:34-42) for a local slot
 __device__ __forceinline__ bool displaced_fp64(const Geom &g, const Slots &s, int sl) {
     const int X = sl % g.Sx, r = sl / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
@@ -1112,7 +1119,7 @@ __device__ __forceinline__ void k_lat_force_fp64_site(int t, const NeighTables &
         else force_sum_fp64<0>(nt, g, s, pt, sl, ti, si, ui, xi, yi, zi, dfi, np, nf, fx, fy, fz);
     }
     s.fx[sl] = fx; s.fy[sl] = fy; s.fz[sl] = fz;
-    if (kick && !hook && lattice_only(in)) {
+    if (kick && !hook && kick_in_lattice_pass(in, sl)) {
         const double c = dt_inv_m_of(sp, ti);
         const double vx = __dadd_rn(s.vx[sl], __dmul_rn(c, fx));
         const double vy = __dadd_rn(s.vy[sl], __dmul_rn(c, fy));
@@ -1266,14 +1273,14 @@ __device__ __forceinline__ void k_lat_force_mixed_site(int t, const NeighTables 
     // a fused body's forces are used only in registers: the next body's firststep is taken here, and
     // the last body of a graph (never fused) stores the forces the state keeps between launches
     if (!fused) { s.fx[sl] = fx; s.fy[sl] = fy; s.fz[sl] = fz; }
-    if (kick && !hook && lattice_only(in)) {
+    if (kick && !hook && kick_in_lattice_pass(in, sl)) {
         const double c = dt_inv_m_of(sp, ti);
         const double vx = __dadd_rn(s.vx[sl], __dmul_rn(c, fx));
         const double vy = __dadd_rn(s.vy[sl], __dmul_rn(c, fy));
         const double vz = __dadd_rn(s.vz[sl], __dmul_rn(c, fz));
-        if (!fuse_next) { s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz; }  // else first_half writes the next v
+        if (!fused) { s.vx[sl] = vx; s.vy[sl] = vy; s.vz[sl] = vz; }  // else first_half writes the next v
         if (variable_dt(sp)) note_vmax2(sp, speed2(vx, vy, vz));
-        if (fuse_next) {
+        if (fused) {
             // the next loop body's firststep for this atom, with the force still in registers (the
             // other threads of this pass still read this atom's u4, so the new record goes to the next
             // body's buffer, u4n)
@@ -1329,7 +1336,9 @@ void launch_lat_force_sites(const LaunchCtx &lc, const Geom &g, Slots s, Inter i
 // inter atoms (src/newton_motion.cpp:57-74)
 __global__ void k_secondstep(Geom g, Slots s, Inter in, StepParams *p, int lattice_mode) {
     const int n_inter = in.cnt[CNT_INTER];
-    const bool lattice = lattice_mode == 1 || (lattice_mode == 2 && !lattice_only(in));
+    // mode 2 (after a kicking force pass): the lattice atoms were kicked by the lattice force pass or,
+    // for the owners of inter-atom pairs, by the owner gather; inter atoms only
+    const bool lattice = lattice_mode == 1;
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
     double v2max = 0.0;
@@ -2068,7 +2077,8 @@ __global__ void __launch_bounds__(kInterThreads) k_inter_eam(const __grid_consta
 // inter-atom pass. The last block to finish resets the list for the next pass; the bits are clear by
 // then.
 template <int KIND>
-__global__ void __launch_bounds__(128) k_inter_owner(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool mixed) {
+__global__ void __launch_bounds__(128) k_inter_owner(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, PotTables pt, bool mixed,
+                                                     StepParams *sp, bool kick) {
     const int n = min(in.cnt[CNT_TOUCHED], in.tcap);
     if (n == 0) return;  // nothing listed: no block writes, so no reset is due
     const int nb = *in.n_bucket;
@@ -2113,12 +2123,26 @@ __global__ void __launch_bounds__(128) k_inter_owner(const __grid_constant__ Nei
         if (lane == 0) {
             if (tj >= 0) {
                 if (KIND == 0) s.rho[j] += acc;
-                else if (KIND == 1) { s.fx[j] += fx; s.fy[j] += fy; s.fz[j] += fz; }
+                else if (KIND == 1) {
+                    const double f0 = s.fx[j] + fx, f1 = s.fy[j] + fy, f2v = s.fz[j] + fz;
+                    s.fx[j] = f0; s.fy[j] = f1; s.fz[j] = f2v;
+                    if (kick) {  // the second half-kick the lattice force pass left to this owner
+                        const double c = dt_inv_m_of(sp, tj);
+                        const double vx = __dadd_rn(s.vx[j], __dmul_rn(c, f0));
+                        const double vy = __dadd_rn(s.vy[j], __dmul_rn(c, f1));
+                        const double vz = __dadd_rn(s.vz[j], __dmul_rn(c, f2v));
+                        s.vx[j] = vx; s.vy[j] = vy; s.vz[j] = vz;
+                        if (variable_dt(sp)) note_vmax2(sp, speed2(vx, vy, vz));
+                    }
+                }
                 else s.e[j] += acc;
             }
-            atomicAnd(&in.touch_bits[j >> 5], ~(1u << (j & 31)));
+            // the density pass's list stays for the force pass of the same positions (its bits tell
+            // the lattice force pass which atoms to leave unkicked); the force and energy passes end it
+            if (KIND != 0) atomicAnd(&in.touch_bits[j >> 5], ~(1u << (j & 31)));
         }
     }
+    if (KIND == 0) return;
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -2130,15 +2154,16 @@ __global__ void __launch_bounds__(128) k_inter_owner(const __grid_constant__ Nei
     }
 }
 template <int KIND>
-void launch_inter_kind(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
+void launch_inter_kind(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, StepParams *sp = nullptr,
+                       bool kick = false) {
     k_inter_eam<KIND><<<lc.num_sms * 4, kInterThreads, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
-    k_inter_owner<KIND><<<lc.num_sms * 4, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed);
+    k_inter_owner<KIND><<<lc.num_sms * 4, 128, 0, lc.stream>>>(*lc.nt, g, s, in, t, mixed, sp, kick);
 }
 void launch_inter_rho(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
     launch_inter_kind<0>(lc, g, s, in, t, mixed);
 }
-void launch_inter_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
-    launch_inter_kind<1>(lc, g, s, in, t, mixed);
+void launch_inter_force(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, StepParams *sp, bool kick) {
+    launch_inter_kind<1>(lc, g, s, in, t, mixed, sp, kick);
 }
 void launch_inter_energy(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed) {
     launch_inter_kind<2>(lc, g, s, in, t, mixed);
