@@ -1771,11 +1771,15 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
         for (int d = 0; d < 3; d++) {
             const int n = in.cnt[CNT_INTER];
             int *cls = in.scratch_i + in.cap;  // 0 stay, 1 lower, 2 higher
+            int leaves = 0;
             for (int a = tid; a < n; a += nthr) {
                 const uint32_t f = is_out_box(g, in.x[a], in.y[a], in.z[a]);
                 cls[a] = (f & lowf[d]) ? 1 : ((f & highf[d]) ? 2 : 0);
+                leaves |= cls[a];
             }
-            __syncthreads();
+            // nobody crosses this dimension's faces (the usual case): the stable partition below
+            // would rewrite the list unchanged
+            if (!__syncthreads_or(leaves)) continue;
             int base = 0;
             for (int which = 0; which < 3; which++) {
                 for (int c0 = 0; c0 < n; c0 += nthr) {
