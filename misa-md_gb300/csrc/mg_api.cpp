@@ -499,6 +499,7 @@ mg_status mg_create(const int64_t phase_space[3], double lattice_const, double r
     g.thr = std::pow(0.2 * lattice_const, 2.0);
     for (int d = 0; d < 3; d++) g.L[d] = phase_space[d] * lattice_const;
     g.inv_h = 2.0 / lattice_const;
+    g.inv_a0 = 1.0 / lattice_const;
     g.h_f = (float) (0.5 * lattice_const);
     g.inv_h_f = (float) g.inv_h;
     g.thr_lo_f = (float) (g.thr * (1.0 - 1e-4));

@@ -67,6 +67,7 @@ struct Geom {
     double thr;              // pow(0.2 a0, 2): displacement threshold of atom::decide
     double L[3];             // periodic lengths
     double inv_h;            // 2 / a0: inverse of the half lattice constant
+    double inv_a0;           // RN(1 / a0): the Voronoi search's estimate of the quotient x / a0
     float inv_h_f;           // 2 / a0 (float)
     float thr_lo_f;          // thr * (1 - 1e-4) in float: FP32 distances below it skip the exact test
     float h_f;               // a0 / 2 (float)
@@ -126,7 +127,7 @@ struct Inter {
     int *gtype, *groot;      // groot: index of the local inter atom this ghost is an image of
     double *gx, *gy, *gz, *gdf;
     // scratch for compaction / sorting (size cap + gcap)
-    int *scratch_i;          // 2 * (cap + gcap)
+    int *scratch_i;          // 3 * cap
     double *scratch_d;       // 13 * cap
     uint64_t *scratch_u;     // cap
     // displaced lattice slots found by the decide scan, in scan order

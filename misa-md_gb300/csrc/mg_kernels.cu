@@ -91,8 +91,8 @@ __device__ __forceinline__ int owner_slot(const Geom &g, int s) {
 // ------------------------------------------------------------------------------------------------
 // Wigner-Seitz mapping (src/lattice/ws_utils.cpp:66-189), one rank: sub-box low corner at 0.
 // ------------------------------------------------------------------------------------------------
-__device__ __forceinline__ void voronoy(double X, double Y, double Z, double lc, long long &cx, long long &cy,
-                                        long long &cz) {
+__device__ __forceinline__ void voronoy_exact(double X, double Y, double Z, double lc, long long &cx, long long &cy,
+                                              long long &cz) {
     const double qx = __ddiv_rn(X, lc), qy = __ddiv_rn(Y, lc), qz = __ddiv_rn(Z, lc);
     cx = llround(qx);
     cy = llround(qy);
@@ -109,9 +109,42 @@ __device__ __forceinline__ void voronoy(double X, double Y, double Z, double lc,
         cz += bz ? 0 : -1;
     }
 }
+// The integers above depend on the quotient q = RN(X / lc) only through three decisions per axis
+// (the nearest integer, the sign of q minus it) and the sign of the bisector-plane sum. The quotient
+// is first estimated as RN(X * RN(1 / lc)), within 3 * 2^-53 |q| of RN(X / lc), i.e. below 4e-10 for
+// |q| < 2^20. Where every decision clears its boundary by kWsMargin, far above that error, the
+// estimate makes the same decisions (the plane sum is the same monotone chain of rounded additions
+// on inputs that moved by less than the margin), so the integers are the exact search's. Sites,
+// half-way points, bisector planes, NaN and huge coordinates take the exact divisions. On this
+// part an FP64 division costs several times a multiply, and the list manager runs these searches
+// in a single block, so their latency is its own.
+constexpr double kWsMargin = 1e-9;
+__device__ __forceinline__ void voronoy(double X, double Y, double Z, const Geom &g, long long &cx, long long &cy,
+                                        long long &cz) {
+    const double qx = __dmul_rn(X, g.inv_a0), qy = __dmul_rn(Y, g.inv_a0), qz = __dmul_rn(Z, g.inv_a0);
+    const double rx = rint(qx), ry = rint(qy), rz = rint(qz);
+    const double dx = __dsub_rn(qx, rx), dy = __dsub_rn(qy, ry), dz = __dsub_rn(qz, rz);
+    const double ax = fabs(dx), ay = fabs(dy), az = fabs(dz);
+    const double plane = __dadd_rn(__dadd_rn(__dadd_rn(ax, ay), az), -0.75);
+    const double amax = fmax(ax, fmax(ay, az)), amin = fmin(ax, fmin(ay, az));
+    const double qmax = fmax(fabs(qx), fmax(fabs(qy), fabs(qz)));
+    const bool clear = amin > kWsMargin && amax < 0.5 - kWsMargin && fabs(plane) > kWsMargin && qmax < 1048576.0;
+    if (!clear) {
+        voronoy_exact(X, Y, Z, g.a0, cx, cy, cz);
+        return;
+    }
+    cx = 2 * (long long) rx;
+    cy = (long long) ry;
+    cz = (long long) rz;
+    if (plane >= 0.0) {
+        cx += dx > 0 ? 1 : -1;
+        cy += dy > 0 ? 0 : -1;
+        cz += dz > 0 ? 0 : -1;
+    }
+}
 __device__ __forceinline__ uint32_t is_out_box(const Geom &g, double x, double y, double z) {
     long long cx, cy, cz;
-    voronoy(x, y, z, g.a0, cx, cy, cz);
+    voronoy(x, y, z, g, cx, cy, cz);
     uint32_t f = kInBox;
     if (cx < 0) f |= kXLow; else if (cx >= g.bx) f |= kXHigh;
     if (cy < 0) f |= kYLow; else if (cy >= g.by) f |= kYHigh;
@@ -120,7 +153,7 @@ __device__ __forceinline__ uint32_t is_out_box(const Geom &g, double x, double y
 }
 // ghost-extended coordinates of the nearest site (ws::getNearLatCoord)
 __device__ __forceinline__ void near_lat_coord(const Geom &g, double x, double y, double z, long long c[3]) {
-    voronoy(x, y, z, g.a0, c[0], c[1], c[2]);
+    voronoy(x, y, z, g, c[0], c[1], c[2]);
     c[0] += g.gx;
     c[1] += g.gy;
     c[2] += g.gz;
@@ -128,7 +161,7 @@ __device__ __forceinline__ void near_lat_coord(const Geom &g, double x, double y
 // ws::findNearLatIndexInSubBox: -1 outside the sub-box
 __device__ __forceinline__ int near_index_in_sub_box(const Geom &g, double x, double y, double z) {
     long long cx, cy, cz;
-    voronoy(x, y, z, g.a0, cx, cy, cz);
+    voronoy(x, y, z, g, cx, cy, cz);
     if (cx < 0 || cy < 0 || cz < 0 || cx >= g.bx || cy >= g.by || cz >= g.bz) return -1;
     return lin(g, (int) cx + g.gx, (int) cy + g.gy, (int) cz + g.gz);
 }
@@ -1656,13 +1689,18 @@ __device__ __forceinline__ void region_fw(const Geom &g, int d, int dir, int lo[
 }
 
 __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, int mask, bool mixed) {
-    __shared__ int sh_n;
     const int tid = threadIdx.x, nthr = blockDim.x;
 
+    // The list counts are read once, by all threads before any is written, and then followed in
+    // registers: every change to them is block-uniform (scan totals), and one global round trip
+    // costs this single block about a microsecond. Thread 0 writes each change back for the
+    // kernels that follow.
+    int n_inter = in.cnt[CNT_INTER], n_ghost = in.cnt[CNT_GHOST];
+    const int n_disp = in.cnt[CNT_DISPLACED];
     // The usual step of a crystal: no inter atom, no ghost image and nothing displaced, so every
     // phase would find its lists empty; what remains is decide voiding the previous step's far list
-    // and the index being empty. The counts are read by all threads before any is written.
-    const bool idle = in.cnt[CNT_INTER] == 0 && in.cnt[CNT_GHOST] == 0 && in.cnt[CNT_DISPLACED] == 0;
+    // and the index being empty.
+    const bool idle = n_inter == 0 && n_ghost == 0 && n_disp == 0;
     __syncthreads();
     if (idle) {
         if (tid == 0) {
@@ -1673,8 +1711,8 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
     }
 
     if (mask & MANAGE_CLEAR_GHOST) {
+        n_ghost = 0;
         if (tid == 0) in.cnt[CNT_GHOST] = 0;
-        __syncthreads();
     }
 
     if (mask & MANAGE_DECIDE) {
@@ -1682,9 +1720,9 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
         if (tid == 0) in.cnt[CNT_FAR] = 0;
         __syncthreads();
         // (i) displaced lattice atoms join the list in scan order (the collected list is ordered)
-        int nd = in.cnt[CNT_DISPLACED];
+        int nd = n_disp;
         if (nd > in.dcap) nd = in.dcap;
-        const int n0 = in.cnt[CNT_INTER];
+        const int n0 = n_inter;
         if (nd > 0) {
             int room = in.cap - n0;
             if (nd > room) { if (tid == 0) set_error(in, MG_DEVERR_INTER_OVERFLOW); nd = room; }
@@ -1703,13 +1741,14 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
                 s.u4[sidx(g, sl)] = vacant_u4();
             }
             __syncthreads();
-            if (tid == 0) in.cnt[CNT_INTER] = n0 + nd;
+            n_inter = n0 + nd;
+            if (tid == 0) in.cnt[CNT_INTER] = n_inter;
         }
         if (tid == 0) in.cnt[CNT_DISPLACED] = 0;
         __syncthreads();
 
         // (ii) recombination with vacancies, first claimant in list order wins
-        const int n = in.cnt[CNT_INTER];
+        const int n = n_inter;
         int *cand = in.scratch_i + in.cap;  // n ints
         for (int a = tid; a < n; a += nthr) {
             const int near = near_index_in_sub_box(g, in.x[a], in.y[a], in.z[a]);
@@ -1722,61 +1761,75 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
         }
         __syncthreads();
         int *won = in.scratch_i + in.cap + in.cap;  // n ints
-        for (int a = tid; a < n; a += nthr) won[a] = (cand[a] >= 0 && in.claim[cand[a]] == a) ? 1 : 0;
-        __syncthreads();
-        for (int a = tid; a < n; a += nthr) if (cand[a] >= 0) in.claim[cand[a]] = INT_MAX;
+        int any_won = 0;
         for (int a = tid; a < n; a += nthr) {
-            if (!won[a]) continue;
-            const int sl = cand[a];
-            s.id[sl] = in.id[a];
-            s.type[sl] = (int8_t) in.type[a];
-            s.x[sl] = in.x[a]; s.y[sl] = in.y[a]; s.z[sl] = in.z[a];
-            s.vx[sl] = in.vx[a]; s.vy[sl] = in.vy[a]; s.vz[sl] = in.vz[a];
-            {
-                const int X = sl % g.Sx, r = sl / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
-                double xs, ys, zs;
-                site_of(g, X, Y, Z, xs, ys, zs);
-                s.u4[sidx(g, sl)] = make_u4(g, in.x[a], in.y[a], in.z[a], xs, ys, zs, in.type[a]);
-            }
-            // A recombined atom may sit up to sqrt(5)/4 a0 from its new site. Every recombined atom
-            // joins this step's far list: the marks on its neighbourhood also make the density pass
-            // rebuild the candidate lists of the groups that can see it (its record did not come
-            // from firststep). The tail pairs the marks add for an atom within 0.2 a0 of its site
-            // are all beyond the cutoff, so they change no sum.
-            {
-                const int q = atomicAdd(&in.cnt[CNT_FAR], 1);
-                if (q < in.fcap) in.far_list[q] = sl;
-                else set_error(in, MG_DEVERR_DISPLACED_OVERFLOW);
-            }
+            won[a] = (cand[a] >= 0 && in.claim[cand[a]] == a) ? 1 : 0;
+            any_won |= won[a];
         }
-        __syncthreads();
-        // stable compaction of the survivors
-        int base = 0;
-        for (int c0 = 0; c0 < n; c0 += nthr) {
-            const int a = c0 + tid;
-            const int keep = (a < n && !won[a]) ? 1 : 0;
-            int ex;
-            const int tot = block_exclusive_scan(keep, ex);
-            if (keep) inter_save(in, a, base + ex);
-            base += tot;
+        const bool recombined = __syncthreads_or(any_won);
+        for (int a = tid; a < n; a += nthr) if (cand[a] >= 0) in.claim[cand[a]] = INT_MAX;
+        // nobody recombined (the usual step): the compaction would rewrite the list unchanged
+        if (recombined) {
+            for (int a = tid; a < n; a += nthr) {
+                if (!won[a]) continue;
+                const int sl = cand[a];
+                s.id[sl] = in.id[a];
+                s.type[sl] = (int8_t) in.type[a];
+                s.x[sl] = in.x[a]; s.y[sl] = in.y[a]; s.z[sl] = in.z[a];
+                s.vx[sl] = in.vx[a]; s.vy[sl] = in.vy[a]; s.vz[sl] = in.vz[a];
+                {
+                    const int X = sl % g.Sx, r = sl / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
+                    double xs, ys, zs;
+                    site_of(g, X, Y, Z, xs, ys, zs);
+                    s.u4[sidx(g, sl)] = make_u4(g, in.x[a], in.y[a], in.z[a], xs, ys, zs, in.type[a]);
+                }
+                // A recombined atom may sit up to sqrt(5)/4 a0 from its new site. Every recombined atom
+                // joins this step's far list: the marks on its neighbourhood also make the density pass
+                // rebuild the candidate lists of the groups that can see it (its record did not come
+                // from firststep). The tail pairs the marks add for an atom within 0.2 a0 of its site
+                // are all beyond the cutoff, so they change no sum.
+                {
+                    const int q = atomicAdd(&in.cnt[CNT_FAR], 1);
+                    if (q < in.fcap) in.far_list[q] = sl;
+                    else set_error(in, MG_DEVERR_DISPLACED_OVERFLOW);
+                }
+            }
+            __syncthreads();
+            // stable compaction of the survivors
+            int base = 0;
+            for (int c0 = 0; c0 < n; c0 += nthr) {
+                const int a = c0 + tid;
+                const int keep = (a < n && !won[a]) ? 1 : 0;
+                int ex;
+                const int tot = block_exclusive_scan(keep, ex);
+                if (keep) inter_save(in, a, base + ex);
+                base += tot;
+            }
+            __syncthreads();
+            for (int a = tid; a < base; a += nthr) inter_restore(in, a, a);
+            n_inter = base;
+            if (tid == 0) in.cnt[CNT_INTER] = base;
         }
-        __syncthreads();
-        for (int a = tid; a < base; a += nthr) inter_restore(in, a, a);
-        if (tid == 0) in.cnt[CNT_INTER] = base;
         __syncthreads();
     }
 
     if (mask & MANAGE_EXCHANGE) {
         const uint32_t lowf[3] = {kXLow, kYLow, kZLow}, highf[3] = {kXHigh, kYHigh, kZHigh};
+        // an atom's out-of-box flags are found once and kept until a partition moves and shifts the
+        // records (each thread keeps the same atoms from one dimension to the next)
+        uint32_t *flags = reinterpret_cast<uint32_t *>(in.scratch_i + 2 * in.cap);
+        bool flags_valid = false;
         for (int d = 0; d < 3; d++) {
-            const int n = in.cnt[CNT_INTER];
+            const int n = n_inter;
             int *cls = in.scratch_i + in.cap;  // 0 stay, 1 lower, 2 higher
             int leaves = 0;
             for (int a = tid; a < n; a += nthr) {
-                const uint32_t f = is_out_box(g, in.x[a], in.y[a], in.z[a]);
+                if (!flags_valid) flags[a] = is_out_box(g, in.x[a], in.y[a], in.z[a]);
+                const uint32_t f = flags[a];
                 cls[a] = (f & lowf[d]) ? 1 : ((f & highf[d]) ? 2 : 0);
                 leaves |= cls[a];
             }
+            flags_valid = true;
             // nobody crosses this dimension's faces (the usual case): the stable partition below
             // would rewrite the list unchanged
             if (!__syncthreads_or(leaves)) continue;
@@ -1802,45 +1855,60 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
             }
             __syncthreads();
             for (int a = tid; a < n; a += nthr) inter_restore(in, a, a);
+            flags_valid = false;
             __syncthreads();
         }
     }
 
     if (mask & MANAGE_BORDER) {
+        // Both directions of a dimension scan the same entries, so each entry's nearest site is found
+        // once per dimension: the lower pass keeps both region tests in mk (bit 0 the region sent
+        // LOWER, bit 1 the one sent HIGHER) for the higher pass. Each thread keeps the same entries in
+        // both passes; cap + gcap ints fit in the 13 * cap doubles of scratch_d.
+        int *mk = reinterpret_cast<int *>(in.scratch_d);
         for (int d = 0; d < 3; d++) {
-            const int n_loc = in.cnt[CNT_INTER];
-            const int n_g0 = in.cnt[CNT_GHOST];
+            const int n_loc = n_inter;
+            const int n_g0 = n_ghost;
             const int total = n_loc + n_g0;
+            int lo[2][3], hi[2][3];
+            region_fw(g, d, 0, lo[0], hi[0]);
+            region_fw(g, d, 1, lo[1], hi[1]);
             for (int dir = 0; dir < 2; dir++) {
-                int lo[3], hi[3];
-                region_fw(g, d, dir, lo, hi);
                 const double sh = (dir == 0) ? g.L[d] : -g.L[d];
-                if (tid == 0) sh_n = in.cnt[CNT_GHOST];
-                __syncthreads();
-                const int base0 = sh_n;
-                int base = base0;
+                int base = n_ghost;
                 for (int c0 = 0; c0 < total; c0 += nthr) {
                     const int e = c0 + tid;
                     int sel = 0;
-                    double px = 0, py = 0, pz = 0;
-                    int ty = 0, root = 0;
                     if (e < total) {
-                        if (e < n_loc) { px = in.x[e]; py = in.y[e]; pz = in.z[e]; ty = in.type[e]; root = e; }
-                        else {
-                            const int q = e - n_loc;
-                            px = in.gx[q]; py = in.gy[q]; pz = in.gz[q]; ty = in.gtype[q]; root = in.groot[q];
+                        if (dir == 0) {
+                            double px, py, pz;
+                            if (e < n_loc) { px = in.x[e]; py = in.y[e]; pz = in.z[e]; }
+                            else { px = in.gx[e - n_loc]; py = in.gy[e - n_loc]; pz = in.gz[e - n_loc]; }
+                            long long c[3];
+                            near_lat_coord(g, px, py, pz, c);
+                            int m = 0;
+                            for (int r = 0; r < 2; r++)
+                                if (c[0] >= lo[r][0] && c[0] < hi[r][0] && c[1] >= lo[r][1] && c[1] < hi[r][1] &&
+                                    c[2] >= lo[r][2] && c[2] < hi[r][2])
+                                    m |= 1 << r;
+                            mk[e] = m;
+                            sel = m & 1;
+                        } else {
+                            sel = (mk[e] >> 1) & 1;
                         }
-                        long long c[3];
-                        near_lat_coord(g, px, py, pz, c);
-                        sel = (c[0] >= lo[0] && c[0] < hi[0] && c[1] >= lo[1] && c[1] < hi[1] && c[2] >= lo[2] &&
-                               c[2] < hi[2]) ? 1 : 0;
                     }
                     int ex;
                     const int tot = block_exclusive_scan(sel, ex);
                     if (sel) {
                         const int q = base + ex;
                         if (q < in.gcap) {
-                            double p3[3] = {px, py, pz};
+                            double p3[3];
+                            int ty, root;
+                            if (e < n_loc) { p3[0] = in.x[e]; p3[1] = in.y[e]; p3[2] = in.z[e]; ty = in.type[e]; root = e; }
+                            else {
+                                const int k = e - n_loc;
+                                p3[0] = in.gx[k]; p3[1] = in.gy[k]; p3[2] = in.gz[k]; ty = in.gtype[k]; root = in.groot[k];
+                            }
                             p3[d] = __dadd_rn(p3[d], sh);
                             in.gx[q] = p3[0]; in.gy[q] = p3[1]; in.gz[q] = p3[2];
                             in.gtype[q] = ty;
@@ -1852,16 +1920,16 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
                     }
                     base += tot;
                 }
-                __syncthreads();
-                if (tid == 0) in.cnt[CNT_GHOST] = base < in.gcap ? base : in.gcap;
+                n_ghost = base < in.gcap ? base : in.gcap;
+                if (tid == 0) in.cnt[CNT_GHOST] = n_ghost;
                 __syncthreads();
             }
         }
     }
 
     if (mask & MANAGE_INDEX) {
-        const int n_loc = in.cnt[CNT_INTER];
-        const int n_gh = in.cnt[CNT_GHOST];
+        const int n_loc = n_inter;
+        const int n_gh = n_ghost;
         const int total = n_loc + n_gh;
         for (int e = tid; e < total; e += nthr) {
             double px, py, pz;

@@ -74,6 +74,14 @@ def test_ws_map_matches_oracle(pkg, orc, wl, potentials, gpu_lib):
     # lattice sites, half-way points and exact bisector-plane points
     s = rng.integers(-2, 27, size=(4000, 3)).astype(float) * a
     pts += [s, s + 0.5 * a, s + 0.25 * a, s + np.array([0.25, 0.25, 0.25]) * a, s - 0.5 * a]
+    # the neighbourhoods of those decision boundaries (nearest integer, sign of the offset, bisector
+    # plane), from one ulp to past the margin within which the search re-divides exactly
+    edge = np.concatenate([s, s + 0.5 * a, s + np.array([0.25, 0.25, 0.25]) * a, s + np.array([0.5, 0.25, 0.0]) * a])
+    pts += [np.nextafter(edge, np.inf), np.nextafter(edge, -np.inf)]
+    for eps in (1e-15, 1e-12, 1e-10, 5e-10, 1e-9, 2e-9, 1e-8):
+        pts.append(edge + eps * a * rng.choice([-1.0, 0.0, 1.0], size=edge.shape))
+    # coordinates beyond 2^20 lattice constants
+    pts.append(rng.uniform(-3e6, 3e6, size=(500, 3)) * a)
     xyz = np.concatenate(pts)
     coords, flags, index = ctx.ws_map(xyz)
     ext, _, oflags, oindex = orc.ws_batch(desc, xyz)
