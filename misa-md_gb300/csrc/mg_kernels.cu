@@ -1688,6 +1688,44 @@ __device__ __forceinline__ void region_fw(const Geom &g, int d, int dir, int lo[
     else { lo[d] = bb[d]; hi[d] = bb[d] + gg[d]; }
 }
 
+// borderInter's entries: the local inter atoms, then the ghost images made so far
+__device__ __forceinline__ void border_entry(const Inter &in, int n_loc, int e, double p3[3], int &ty, int &root) {
+    if (e < n_loc) {
+        p3[0] = in.x[e]; p3[1] = in.y[e]; p3[2] = in.z[e];
+        ty = in.type[e];
+        root = e;
+    } else {
+        const int k = e - n_loc;
+        p3[0] = in.gx[k]; p3[1] = in.gy[k]; p3[2] = in.gz[k];
+        ty = in.gtype[k];
+        root = in.groot[k];
+    }
+}
+// bit r set: the entry's nearest site lies in the region sent to direction r
+__device__ __forceinline__ int border_regions(const Geom &g, const int lo[2][3], const int hi[2][3], const double p3[3]) {
+    long long c[3];
+    near_lat_coord(g, p3[0], p3[1], p3[2], c);
+    int m = 0;
+    for (int r = 0; r < 2; r++)
+        if (c[0] >= lo[r][0] && c[0] < hi[r][0] && c[1] >= lo[r][1] && c[1] < hi[r][1] && c[2] >= lo[r][2] &&
+            c[2] < hi[r][2])
+            m |= 1 << r;
+    return m;
+}
+// ghost image q of an entry, shifted by sh along d (past the capacity: the overflow error)
+__device__ __forceinline__ void border_put(Inter &in, int q, const double p3[3], int d, double sh, int ty, int root) {
+    if (q >= in.gcap) {
+        set_error(in, MG_DEVERR_GHOST_OVERFLOW);
+        return;
+    }
+    double p[3] = {p3[0], p3[1], p3[2]};
+    p[d] = __dadd_rn(p[d], sh);
+    in.gx[q] = p[0]; in.gy[q] = p[1]; in.gz[q] = p[2];
+    in.gtype[q] = ty;
+    in.groot[q] = root;
+    in.gdf[q] = 0.0;
+}
+
 __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, int mask, bool mixed) {
     const int tid = threadIdx.x, nthr = blockDim.x;
 
@@ -1861,18 +1899,37 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
     }
 
     if (mask & MANAGE_BORDER) {
-        // Both directions of a dimension scan the same entries, so each entry's nearest site is found
-        // once per dimension: the lower pass keeps both region tests in mk (bit 0 the region sent
-        // LOWER, bit 1 the one sent HIGHER) for the higher pass. Each thread keeps the same entries in
-        // both passes; cap + gcap ints fit in the 13 * cap doubles of scratch_d.
+        // Both directions of a dimension send from the same entries, so each entry's nearest site is
+        // found once per dimension. With one chunk of entries (the usual case) both directions share
+        // one scan: the lower direction's selections are counted in the low 16 bits of the packed
+        // sums, the higher's above them. With more, the lower pass keeps both region tests in mk
+        // (bit 0 the region sent LOWER, bit 1 the one sent HIGHER) for the higher pass; each thread
+        // keeps the same entries in both passes, and cap + gcap ints fit in the 13 * cap doubles of
+        // scratch_d.
         int *mk = reinterpret_cast<int *>(in.scratch_d);
         for (int d = 0; d < 3; d++) {
             const int n_loc = n_inter;
-            const int n_g0 = n_ghost;
-            const int total = n_loc + n_g0;
+            const int total = n_loc + n_ghost;
             int lo[2][3], hi[2][3];
             region_fw(g, d, 0, lo[0], hi[0]);
             region_fw(g, d, 1, lo[1], hi[1]);
+            if (total <= nthr) {
+                double p3[3] = {0.0, 0.0, 0.0};
+                int ty = 0, root = 0, m = 0;
+                if (tid < total) {
+                    border_entry(in, n_loc, tid, p3, ty, root);
+                    m = border_regions(g, lo, hi, p3);
+                }
+                int ex;
+                const int tot = block_exclusive_scan((m & 1) | ((m & 2) << 15), ex);
+                const int base1 = min(n_ghost + (tot & 0xffff), in.gcap);
+                if (m & 1) border_put(in, n_ghost + (ex & 0xffff), p3, d, g.L[d], ty, root);
+                if (m & 2) border_put(in, base1 + (ex >> 16), p3, d, -g.L[d], ty, root);
+                n_ghost = min(base1 + (tot >> 16), in.gcap);
+                if (tid == 0) in.cnt[CNT_GHOST] = n_ghost;
+                __syncthreads();
+                continue;
+            }
             for (int dir = 0; dir < 2; dir++) {
                 const double sh = (dir == 0) ? g.L[d] : -g.L[d];
                 int base = n_ghost;
@@ -1881,16 +1938,10 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
                     int sel = 0;
                     if (e < total) {
                         if (dir == 0) {
-                            double px, py, pz;
-                            if (e < n_loc) { px = in.x[e]; py = in.y[e]; pz = in.z[e]; }
-                            else { px = in.gx[e - n_loc]; py = in.gy[e - n_loc]; pz = in.gz[e - n_loc]; }
-                            long long c[3];
-                            near_lat_coord(g, px, py, pz, c);
-                            int m = 0;
-                            for (int r = 0; r < 2; r++)
-                                if (c[0] >= lo[r][0] && c[0] < hi[r][0] && c[1] >= lo[r][1] && c[1] < hi[r][1] &&
-                                    c[2] >= lo[r][2] && c[2] < hi[r][2])
-                                    m |= 1 << r;
+                            double p3[3];
+                            int ty, root;
+                            border_entry(in, n_loc, e, p3, ty, root);
+                            const int m = border_regions(g, lo, hi, p3);
                             mk[e] = m;
                             sel = m & 1;
                         } else {
@@ -1900,23 +1951,10 @@ __global__ void __launch_bounds__(kManageThreads) k_inter_manage(const __grid_co
                     int ex;
                     const int tot = block_exclusive_scan(sel, ex);
                     if (sel) {
-                        const int q = base + ex;
-                        if (q < in.gcap) {
-                            double p3[3];
-                            int ty, root;
-                            if (e < n_loc) { p3[0] = in.x[e]; p3[1] = in.y[e]; p3[2] = in.z[e]; ty = in.type[e]; root = e; }
-                            else {
-                                const int k = e - n_loc;
-                                p3[0] = in.gx[k]; p3[1] = in.gy[k]; p3[2] = in.gz[k]; ty = in.gtype[k]; root = in.groot[k];
-                            }
-                            p3[d] = __dadd_rn(p3[d], sh);
-                            in.gx[q] = p3[0]; in.gy[q] = p3[1]; in.gz[q] = p3[2];
-                            in.gtype[q] = ty;
-                            in.groot[q] = root;
-                            in.gdf[q] = 0.0;
-                        } else {
-                            set_error(in, MG_DEVERR_GHOST_OVERFLOW);
-                        }
+                        double p3[3];
+                        int ty, root;
+                        border_entry(in, n_loc, e, p3, ty, root);
+                        border_put(in, base + ex, p3, d, sh, ty, root);
                     }
                     base += tot;
                 }

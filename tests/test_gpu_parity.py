@@ -257,9 +257,12 @@ def test_inter_atom_runs_are_reproducible(pkg, wl, potentials, gpu_lib, prec):
 # migration tier: decide, exchangeInter, borderInter bit for bit
 # ------------------------------------------------------------------------------------------------
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
-def test_decide_exchange_border_bit_exact(pkg, orc, wl, potentials, gpu_lib, prec):
-    cells = (8, 9, 10)
-    atoms = displaced_state(wl, cells, seed=17, n_move=60)
+@pytest.mark.parametrize("cells,n_move", [((8, 9, 10), 60), ((20, 20, 20), 8000)])
+def test_decide_exchange_border_bit_exact(pkg, orc, wl, potentials, gpu_lib, prec, cells, n_move):
+    """The list phases one at a time against the oracle's. The 20^3 box moves 8,000 of its 16,000
+    atoms: about 1,400 stay inter atoms, with about 1,700 ghost images, so the list and the entries of
+    every border pass span more than one chunk of the list manager's block (1,024 threads)."""
+    atoms = displaced_state(wl, cells, seed=17, n_move=n_move)
     ctx, ref = make_pair(pkg, orc, wl, potentials["fe"], cells, atoms, precision=prec)
     for phase, fn in ((1, ref.decide), (2, ref.exchange_inter), (3, ref.border_inter)):
         ctx.phase(phase)
