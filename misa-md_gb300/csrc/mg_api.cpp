@@ -59,6 +59,7 @@ struct mg_context {
     bool prepared = false;
     std::string err;
     mg_atom_element *d_aos = nullptr;
+    mg_atom_element *d_aos_in = nullptr;  // the overlapped host step's input, kept for a full rerun
     double *d_partials = nullptr;
     double *d_thermo = nullptr;
     double *d_samples = nullptr;    // stage-machine thermo samples (8 doubles each)
@@ -1256,8 +1257,167 @@ mg_status mg_clear_errors(mg_context *ctx) {
     return MG_OK;
 }
 
+// One loop body from and to the host slot array with the copies out overlapped by the copies in (fixed
+// dt, no inter atoms in; the host link carries both directions at once). The in-chunks arrive bottom to
+// top into a kept input buffer. Each is unpacked and takes its firststep, decide's own-site case
+// (launch_spec_decide) and its in-plane ghost copy. A density slab runs once every plane within 3 of it
+// has arrived, a force slab once the density slabs beside it have run, and its finished planes are packed
+// and copied out at once while later chunks are still coming in. The thin slabs at the periodic z seam
+// (two of 4 planes at each end) wait for the ghost planes, copied after the last chunk. Per atom the
+// kernels and their order are those of the unpipelined path, so the result is bit-identical to it. If a
+// chunk's decide met a displaced atom that does not go straight back to its own site, the step is void:
+// it runs again in full from the kept input, as mg_upload + one loop body + mg_download would.
+// S in-chunks and SS >= 6 density slabs, SS <= bz / 4, at least 32 sites of a parity per plane.
+static mg_status step_host_overlapped(mg_context *ctx, mg_atom_element *atoms, mg_atom_element *inter,
+                                      int64_t inter_cap, int64_t *n_inter, int S, int SS) {
+    const Geom &g = ctx->g;
+    if (!ctx->copy_in) MG_CK(cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
+    if (!ctx->copy_out) MG_CK(cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));
+    const size_t n_ev = static_cast<size_t>(S + SS + 8);
+    while (ctx->pipe_ev.size() < n_ev) {
+        cudaEvent_t e;
+        MG_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->pipe_ev.push_back(e);
+    }
+    mg_status st;
+    if ((st = ensure_aos(ctx)) != MG_OK) return st;
+    if (!ctx->d_aos_in) MG_CK(dalloc(ctx, &ctx->d_aos_in, static_cast<size_t>(g.n_slots)));
+    const LaunchCtx lc = ctx->lc();
+    const bool mx = ctx->mixed();
+    const int K = g.bz;
+    const int64_t plane = static_cast<int64_t>(g.Sx) * g.Sy;  // slots per z plane
+    const int pp = g.by * g.nxh;                               // sites of one parity per local plane
+    const size_t rec = sizeof(mg_atom_element);
+    size_t ev = 0;
+    // in-chunks of whole planes, the last one thin (4 planes)
+    auto local_plane_bound = [&](int c) {
+        if (c == S) return K;
+        if (c == S - 1) return K - 4;
+        return static_cast<int>((static_cast<int64_t>(c) * (K - 4)) / (S - 1));
+    };
+    // density and force slabs: kb[c] local planes, u[c] sites (whole 32-site groups)
+    std::vector<int> kb(SS + 1), u(SS + 1);
+    for (int c = 0; c <= SS; c++) {
+        if (c <= 2) kb[c] = 4 * c;
+        else if (c >= SS - 2) kb[c] = K - 4 * (SS - c);
+        else kb[c] = 8 + static_cast<int>((static_cast<int64_t>(c - 2) * (K - 16)) / (SS - 4));
+        u[c] = c == SS ? g.n_local_half : static_cast<int>(((static_cast<int64_t>(kb[c]) * pp) >> 5) << 5);
+    }
+    auto last_plane = [&](int c) { return (u[c + 1] - 1) / pp; };    // the plane of slab c's last site
+    auto planes_below = [&](int c) { return u[c] / pp; };           // planes wholly below u[c]
+    auto planes_from = [&](int c) { return (u[c] + pp - 1) / pp; };  // first plane wholly at or above u[c]
+
+    // head: the copies wait for everything already on the library stream
+    MG_CK(cudaEventRecord(ctx->pipe_ev[ev], ctx->stream));
+    MG_CK(cudaStreamWaitEvent(ctx->copy_in, ctx->pipe_ev[ev++], 0));
+    launch_set_counts(lc, ctx->in, 0);
+    launch_step_head(lc, ctx->d_sp);
+    launch_far_clear(lc, g, ctx->in);  // the previous far list's marks, which decide clears
+    launch_spec_begin(lc, ctx->in);
+    std::vector<size_t> in_ev(S);
+    std::vector<int64_t> cs0(S), cs1(S);
+    for (int c = 0; c < S; c++) {
+        const int z0 = c == 0 ? 0 : g.gz + local_plane_bound(c);
+        const int z1 = c == S - 1 ? g.Sz : g.gz + local_plane_bound(c + 1);
+        cs0[c] = z0 * plane;
+        cs1[c] = z1 * plane;
+        MG_CK(cudaMemcpyAsync(ctx->d_aos_in + cs0[c], atoms + cs0[c], static_cast<size_t>(cs1[c] - cs0[c]) * rec,
+                              cudaMemcpyHostToDevice, ctx->copy_in));
+        in_ev[c] = ev;
+        MG_CK(cudaEventRecord(ctx->pipe_ev[ev++], ctx->copy_in));
+    }
+    // out: pack the slot planes [z0, z1) and copy them on copy_out
+    auto flush = [&](int z0, int z1) -> mg_status {
+        if (z1 <= z0) return MG_OK;
+        const int64_t s0 = z0 * plane, s1 = z1 * plane;
+        launch_pack_aos(lc, g, ctx->d_aos, ctx->s, PACK_ALL, mx, static_cast<int>(s0), static_cast<int>(s1));
+        MG_CK(cudaEventRecord(ctx->pipe_ev[ev], ctx->stream));
+        MG_CK(cudaStreamWaitEvent(ctx->copy_out, ctx->pipe_ev[ev++], 0));
+        MG_CK(cudaMemcpyAsync(atoms + s0, ctx->d_aos + s0, static_cast<size_t>(s1 - s0) * rec, cudaMemcpyDeviceToHost,
+                              ctx->copy_out));
+        return MG_OK;
+    };
+    auto rho_slab = [&](int c) { launch_lat_rho_sites(lc, g, ctx->s, ctx->in, ctx->pt, mx, u[c], u[c + 1], true); };
+    auto force_slab = [&](int c) {
+        launch_lat_force_sites(lc, g, ctx->s, ctx->in, ctx->pt, ctx->d_sp, true, mx, u[c], u[c + 1], true);
+    };
+    int next_rho = 1, next_force = 2;
+    int df_hi = planes_from(1);                 // in-plane ghosts of planes [planes_from(1), df_hi) have their df
+    const int out_lo = g.gz + planes_from(2);   // slot planes [out_lo, out_hi) are on their way out
+    int out_hi = out_lo;
+    for (int c = 0; c < S; c++) {
+        MG_CK(cudaStreamWaitEvent(ctx->stream, ctx->pipe_ev[in_ev[c]], 0));
+        launch_unpack_aos(lc, g, ctx->d_aos_in, ctx->s, ctx->in, ctx->types_ok_mask, mx, static_cast<int>(cs0[c]),
+                          static_cast<int>(cs1[c]));
+        const int k0 = c == 0 ? 0 : local_plane_bound(c), k1 = local_plane_bound(c + 1);
+        const int t0 = k0 * g.by * g.bx, t1 = k1 * g.by * g.bx;
+        launch_firststep(lc, g, ctx->s, ctx->in, ctx->d_sp, true, t0, t1);
+        launch_spec_decide(lc, g, ctx->s, ctx->in, t0, t1);
+        launch_ghost_copy_planes(lc, g, ctx->s, k0, k1);
+        // slabs 1 .. SS - 2 in order once the planes within 3 of them are in; then the forces of slabs
+        // 2 .. SS - 3 whose neighbour slabs have their density, and their finished planes go out
+        while (next_rho <= SS - 2 && last_plane(next_rho) + 3 < k1) {
+            rho_slab(next_rho);
+            const int hi = planes_below(next_rho + 1);
+            launch_ghost_df_planes(lc, g, ctx->s, ctx->in, mx, df_hi, hi);
+            df_hi = std::max(df_hi, hi);
+            next_rho++;
+            while (next_force <= SS - 3 && next_force + 1 < next_rho) {
+                force_slab(next_force);
+                const int z_to = g.gz + planes_below(next_force + 1);
+                if ((st = flush(out_hi, z_to)) != MG_OK) return st;
+                out_hi = std::max(out_hi, z_to);
+                next_force++;
+            }
+        }
+    }
+    if (next_rho != SS - 1 || next_force != SS - 2) {
+        ctx->err = "overlapped host step: slab schedule incomplete";
+        return MG_ERR_STATE;
+    }
+    // the seam: ghost planes, the end slabs' density and ghost df, then their forces
+    launch_ghost_copy_planes(lc, g, ctx->s, -1, -1);
+    rho_slab(0);
+    rho_slab(SS - 1);
+    launch_ghost_df_planes(lc, g, ctx->s, ctx->in, mx, 0, planes_from(1));
+    launch_ghost_df_planes(lc, g, ctx->s, ctx->in, mx, df_hi, K);
+    launch_ghost_df_planes(lc, g, ctx->s, ctx->in, mx, -1, -1);
+    if (mx) launch_skin_advance(lc, ctx->s);  // after the last density slab
+    force_slab(1);
+    force_slab(0);
+    if ((st = flush(0, out_lo)) != MG_OK) return st;
+    force_slab(SS - 2);
+    force_slab(SS - 1);
+    if ((st = flush(out_hi, g.Sz)) != MG_OK) return st;
+    seq_eam_force_tail(ctx, true, nullptr);
+    if ((st = check_launch(ctx)) != MG_OK) return st;
+
+    int cnt[CNT_WORDS];
+    MG_CK(cudaMemcpyAsync(cnt, ctx->in.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_CK(cudaStreamSynchronize(ctx->stream));
+    MG_CK(cudaStreamSynchronize(ctx->copy_out));
+    ctx->prepared = true;
+    ctx->vmax_stale = true;
+    ctx->energy_valid = false;
+    if (cnt[CNT_SPEC_VOID]) {
+        // the whole loop body again from the kept input (the step head has run once already)
+        launch_unpack_aos(lc, g, ctx->d_aos_in, ctx->s, ctx->in, ctx->types_ok_mask, mx);
+        launch_set_counts(lc, ctx->in, 0);
+        seq_firststep(ctx, true, nullptr);
+        seq_compute_eam(ctx, true, true, MANAGE_DECIDE | MANAGE_CLEAR_GHOST | MANAGE_EXCHANGE | MANAGE_BORDER, nullptr);
+        if ((st = check_launch(ctx)) != MG_OK) return st;
+        if ((st = mg_download(ctx, atoms, g.n_slots, inter, inter_cap, n_inter)) != MG_OK) return st;
+        uint32_t bits = 0;
+        if ((st = read_device_errors(ctx, &bits)) != MG_OK) return st;
+        return status_from_bits(ctx, bits);
+    }
+    *n_inter = 0;
+    return status_from_bits(ctx, static_cast<uint32_t>(cnt[CNT_ERRORS]));
+}
+
 // One loop body from and to the host slot array with the copies overlapped by the step (fixed dt, no
-// inter atoms in). The slot grid is cut into z-slabs of whole planes:
+// inter atoms in), for boxes too thin for the overlapped path above. The slot grid is cut into z-slabs
+// of whole planes:
 //   in:  slab c is copied in on copy_in while slab c - 1 is unpacked and takes its firststep;
 //   out: density and force run slab by slab; once a slab's planes are final they are packed and copied
 //        out on copy_out while the next slabs compute.
@@ -1269,6 +1429,10 @@ static mg_status step_host_pipelined(mg_context *ctx, mg_atom_element *atoms, mg
                                      int64_t *n_inter) {
     const Geom &g = ctx->g;
     const int S = std::min(ctx->host_chunks, g.bz);
+    {
+        const int SS = std::min(S, g.bz / 4);
+        if (S >= 3 && SS >= 6 && g.by * g.nxh >= 32) return step_host_overlapped(ctx, atoms, inter, inter_cap, n_inter, S, SS);
+    }
     if (!ctx->copy_in) MG_CK(cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
     if (!ctx->copy_out) MG_CK(cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));
     const size_t n_ev = static_cast<size_t>(2 * S + 4);

@@ -29,9 +29,10 @@ constexpr uint32_t kInBox = 0, kXLow = 1u, kXHigh = 2u, kYLow = 4u, kYHigh = 8u,
 // CNT_DISP_RAW: displaced slots counted by firststep this step (0 lets the collection kernels skip)
 // CNT_TOUCHED: lattice owners listed by an inter-atom pass for the ordered owner gather that follows;
 // CNT_TOUCH_DONE: blocks of that gather finished (the last one resets both words)
+// CNT_SPEC_VOID: the overlapped host step met a displaced atom whose decide it cannot take per chunk
 enum {
     CNT_INTER = 0, CNT_GHOST = 1, CNT_DISPLACED = 2, CNT_ERRORS = 3, CNT_FAR = 4, CNT_DISP_RAW = 5, CNT_TOUCHED = 6,
-    CNT_TOUCH_DONE = 7, CNT_WORDS = 8
+    CNT_TOUCH_DONE = 7, CNT_SPEC_VOID = 8, CNT_WORDS = 9
 };
 
 inline double atom_mass(int type) {  // src/types/atom_types.h:42-53
@@ -291,6 +292,15 @@ void launch_skin_dirty(const LaunchCtx &lc, Slots s);
 // forward df for the ghost slots inside local planes [k0, k1), or (k0 < 0) the ghost planes below and
 // above the box plus the ghost inter atoms
 void launch_ghost_df_planes(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, bool mixed, int k0, int k1);
+// the lattice ghost copy for the ghost slots inside the local planes [k0, k1), or (k0 < 0) for the
+// ghost planes below and above the box
+void launch_ghost_copy_planes(const LaunchCtx &lc, const Geom &g, Slots s, int k0, int k1);
+// The overlapped host step's decide on the local indices [t0, t1) after their firststep (no inter atoms
+// in): a displaced atom nearest its own site goes into the list and back, leaving a new displacement
+// record and a far-list entry whose neighbourhood is marked here; any other sets CNT_SPEC_VOID.
+void launch_spec_decide(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, int t0, int t1);
+// CNT_FAR = 0 and CNT_SPEC_VOID = 0 (after the previous far list's marks are cleared)
+void launch_spec_begin(const LaunchCtx &lc, Inter in);
 void launch_lat_df(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, PotTables t, bool mixed, bool hook);
 // fuse_next (mixed form, kick, fixed dt): after the second half-kick each lattice atom also takes the
 // next step's firststep (into u4n), when no inter atoms exist

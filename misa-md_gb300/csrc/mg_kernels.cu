@@ -671,10 +671,7 @@ __device__ __forceinline__ int ghost_slot(const Geom &g, int t) {
     return lin(g, X, Y, Z);
 }
 
-__global__ void k_ghost_copy(Geom g, Slots s) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.n_ghost_slots) return;
-    const int gs = ghost_slot(g, t);
+__device__ __forceinline__ void ghost_copy_one(const Geom &g, const Slots &s, int gs) {
     const int X = gs % g.Sx, r = gs / g.Sx, Y = r % g.Sy, Z = r / g.Sy;
     int sx, sy, sz;
     const int os = lin(g, wrap_axis(X, g.gx, g.bx, sx), wrap_axis(Y, g.gy, g.by, sy), wrap_axis(Z, g.gz, g.bz, sz));
@@ -685,9 +682,44 @@ __global__ void k_ghost_copy(Geom g, Slots s) {
     s.z[gs] = sz ? __dadd_rn(oz, sz > 0 ? g.L[2] : -g.L[2]) : oz;
     s.u4[sidx(g, gs)] = s.u4[sidx(g, os)];
 }
+__global__ void k_ghost_copy(Geom g, Slots s) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n_ghost_slots) return;
+    ghost_copy_one(g, s, ghost_slot(g, t));
+}
 void launch_ghost_copy(const LaunchCtx &lc, const Geom &g, Slots s, bool) {
     const int b = 256, n = (g.n_ghost_slots + b - 1) / b;
     k_ghost_copy<<<n, b, 0, lc.stream>>>(g, s);
+}
+// The ghost slots inside the local planes [k0, k1) (y-ghost rows, then x-ghost columns of each plane;
+// their owners lie in the same plane), or (k0 < 0) the ghost planes below and above the box, whose
+// owners are the top and bottom local planes. Together the calls cover every ghost slot once.
+__global__ void k_ghost_copy_planes(Geom g, Slots s, int k0, int k1) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k0 < 0) {
+        if (t < 2 * g.gz * g.Sy * g.Sx) ghost_copy_one(g, s, ghost_slot(g, t));  // the z-ghost planes come first
+        return;
+    }
+    const int rows = 2 * g.gy * g.Sx, per = rows + 2 * g.gx * g.by;
+    if (t >= (k1 - k0) * per) return;
+    const int Z = g.gz + k0 + t / per, v = t % per;
+    int X, Y;
+    if (v < rows) {
+        const int yy = v / g.Sx;
+        Y = yy < g.gy ? yy : yy + g.by;
+        X = v % g.Sx;
+    } else {
+        const int w = v - rows, xx = w % (2 * g.gx);
+        X = xx < g.gx ? xx : xx + g.bx;
+        Y = g.gy + w / (2 * g.gx);
+    }
+    ghost_copy_one(g, s, lin(g, X, Y, Z));
+}
+void launch_ghost_copy_planes(const LaunchCtx &lc, const Geom &g, Slots s, int k0, int k1) {
+    const int b = 256;
+    const int work = k0 < 0 ? 2 * g.gz * g.Sy * g.Sx : (k1 - k0) * (2 * g.gy * g.Sx + 2 * g.gx * g.by);
+    if (work <= 0) return;
+    k_ghost_copy_planes<<<(work + b - 1) / b, b, 0, lc.stream>>>(g, s, k0, k1);
 }
 
 // forward df (DfEmbedPacker, src/pack/df_embed_packer.cpp): lattice ghosts and ghost inter atoms
@@ -2316,6 +2348,53 @@ void launch_far_rebuild(const LaunchCtx &lc, const Geom &g, Slots s, Inter in) {
     const int b = 256;
     k_far_scan<<<(g.n_local + b - 1) / b, b, 0, lc.stream>>>(g, s, in);
     launch_far_mark(lc, g, in);
+}
+
+// ------------------------------------------------------------------------------------------------
+// decide per chunk of planes, for the host step that overlaps its copies out with its copies in.
+// With no inter atoms at the start of the step, decide (src/atom.cpp:21-84) puts every displaced atom
+// into the list in scan order and then, in list order, moves each one whose nearest site is a vacant
+// in-box slot into that slot. When every displaced atom's nearest site is its own slot, each is the
+// only claimant of the slot it just vacated, so it goes back at once with its id, type, position and
+// velocity: the step then differs from one without it only in the atom's displacement record, which
+// recombination rewrites from the position, and in its far-list entry and neighbourhood marks. Those
+// are made here, per chunk, before any density pass reads the neighbourhood. A displaced atom nearest
+// another site (or outside the sub-box), or a full far list, voids the overlapped step instead: the
+// host then runs the whole step again from its input.
+// ------------------------------------------------------------------------------------------------
+__global__ void k_spec_begin(Inter in) {
+    in.cnt[CNT_FAR] = 0;
+    in.cnt[CNT_SPEC_VOID] = 0;
+}
+void launch_spec_begin(const LaunchCtx &lc, Inter in) { k_spec_begin<<<1, 1, 0, lc.stream>>>(in); }
+
+__global__ void k_spec_decide(const __grid_constant__ NeighTables nt, Geom g, Slots s, Inter in, int t0, int t1) {
+    if (in.cnt[CNT_DISP_RAW] == 0) return;  // nothing displaced so far this step
+    for (int t = t0 + blockIdx.x * blockDim.x + threadIdx.x; t < t1; t += gridDim.x * blockDim.x) {
+        if (!in.dflag[t]) continue;
+        int i, j, k;
+        const int sl = local_slot(g, t, i, j, k);
+        const double x = s.x[sl], y = s.y[sl], z = s.z[sl];
+        if (near_index_in_sub_box(g, x, y, z) != sl) {
+            atomicExch(&in.cnt[CNT_SPEC_VOID], 1);
+            continue;
+        }
+        const int q = atomicAdd(&in.cnt[CNT_FAR], 1);
+        if (q >= in.fcap) {
+            atomicExch(&in.cnt[CNT_SPEC_VOID], 1);
+            continue;
+        }
+        double xs, ys, zs;
+        site_of(g, i + g.gx, j + g.gy, k + g.gz, xs, ys, zs);
+        s.u4[sidx(g, sl)] = make_u4(g, x, y, z, xs, ys, zs, s.type[sl]);
+        in.far_list[q] = sl;
+        mark_far_neighbourhoods(nt, g, in, q, q + 1, 1, 0, 1);
+    }
+}
+void launch_spec_decide(const LaunchCtx &lc, const Geom &g, Slots s, Inter in, int t0, int t1) {
+    if (t1 <= t0) return;
+    const int b = 256, n = std::min((t1 - t0 + b - 1) / b, lc.num_sms * 4);
+    k_spec_decide<<<n, b, 0, lc.stream>>>(*lc.nt, g, s, in, t0, t1);
 }
 
 

@@ -81,6 +81,95 @@ def test_pipelined_step_host_falls_back_when_decide_moves_atoms(pkg, wl, potenti
     cu.close()
 
 
+def _push(a, wl, cells, picks, d):
+    loc = wl.local_slot_indices(cells, RCF)
+    for k in picks:
+        a["x"][loc[k]] += A0 * np.asarray(d, dtype=float)
+
+
+def _plane_picks(cells, planes, per_plane=3):
+    """Local indices (k, j, i order) of a few atoms in each of the given local z planes."""
+    nxy = 2 * cells[0] * cells[1]
+    rng = np.random.default_rng(5)
+    return [p * nxy + int(q) for p in planes for q in rng.choice(nxy, size=per_plane, replace=False)]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_overlapped_step_host_with_own_site_displacements(pkg, wl, potentials, gpu_lib, precision):
+    """The overlapped path (40 planes, 8 density slabs): atoms pushed 0.26 a0 along x leave their
+    sites but stay nearest them, so each step's decide puts them into the list and straight back.
+    They sit in the planes at both z seams, at chunk edges and in the middle; four calls against the
+    unpipelined path, bit for bit, with no inter atom left."""
+    cells = (8, 8, 40)
+    a0, _ = _prepared_state(pkg, wl, cells, potentials["fecuni"], precision)
+    _push(a0, wl, cells, _plane_picks(cells, (0, 1, 2, 4, 5, 13, 20, 21, 34, 36, 37, 38, 39)), (0.26, 0.0, 0.0))
+    got, want = a0.copy(), a0.copy()
+    cp = _ctx(pkg, cells, potentials["fecuni"], precision, 8)
+    cu = _ctx(pkg, cells, potentials["fecuni"], precision, 0)
+    inter_p = np.zeros(64, dtype=pkg.ATOM_DTYPE)
+    inter_u = np.zeros(64, dtype=pkg.ATOM_DTYPE)
+    np_, nu = 0, 0
+    for _ in range(4):
+        np_ = cp.step_host(got, inter_p, np_, 1)
+        nu = cu.step_host(want, inter_u, nu, 1)
+        assert np_ == nu == 0
+        assert got.tobytes() == want.tobytes()
+    cp.close()
+    cu.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("plane", [2, 19, 39])
+def test_overlapped_step_host_reruns_when_decide_keeps_an_atom(pkg, wl, potentials, gpu_lib, precision, plane):
+    """The overlapped path with one atom pushed 0.3 a0 along (1, 1, 1), nearest an occupied neighbour's
+    site, beside own-site displacements: the chunk's decide voids the overlapped step, which runs
+    again in full from its input. The result, the inter atom included, equals the unpipelined path."""
+    cells = (8, 8, 40)
+    a0, _ = _prepared_state(pkg, wl, cells, potentials["fecuni"], precision)
+    _push(a0, wl, cells, _plane_picks(cells, (1, 20, 38), per_plane=2), (-0.26, 0.0, 0.0))
+    nxy = 2 * cells[0] * cells[1]
+    _push(a0, wl, cells, [plane * nxy + 77], (0.3, 0.3, 0.3))
+    got, want = a0.copy(), a0.copy()
+    cp = _ctx(pkg, cells, potentials["fecuni"], precision, 8)
+    cu = _ctx(pkg, cells, potentials["fecuni"], precision, 0)
+    inter_p = np.zeros(64, dtype=pkg.ATOM_DTYPE)
+    inter_u = np.zeros(64, dtype=pkg.ATOM_DTYPE)
+    np_ = cp.step_host(got, inter_p, 0, 1)
+    nu = cu.step_host(want, inter_u, 0, 1)
+    assert np_ == nu == 1
+    assert got.tobytes() == want.tobytes()
+    assert inter_p[:1].tobytes() == inter_u[:1].tobytes()
+    np_ = cp.step_host(got, inter_p, np_, 1)
+    nu = cu.step_host(want, inter_u, nu, 1)
+    assert np_ == nu and got.tobytes() == want.tobytes()
+    cp.close()
+    cu.close()
+
+
+def test_overlapped_step_host_matches_oracle(pkg, orc, wl, potentials, gpu_lib):
+    """Three overlapped FP64 calls (32 planes, 8 density slabs) against three oracle loop bodies."""
+    cells = (8, 8, 32)
+    a0, _ = _prepared_state(pkg, wl, cells, potentials["fe"], "fp64", alloy=False)
+    _push(a0, wl, cells, _plane_picks(cells, (0, 15, 31), per_plane=2), (0.0, 0.26, 0.0))
+    got = a0.copy()
+    cp = _ctx(pkg, cells, potentials["fe"], "fp64", 8)
+    inter = np.zeros(16, dtype=pkg.ATOM_DTYPE)
+    n = 0
+    for _ in range(3):
+        n = cp.step_host(got, inter, n, 1)
+    ref = orc.OracleSim(cells, A0, RCF, potentials["fe"], dt=0.001)
+    ref.set_atoms(a0)
+    ref.exchange_atom_first()
+    ref.simulate(3)
+    w = ref.get_atoms()
+    loc = wl.local_slot_indices(cells, RCF)
+    assert n == ref.get_inter().size == 0
+    assert np.array_equal(got["type"][loc], w["type"][loc]) and np.array_equal(got["id"][loc], w["id"][loc])
+    assert np.abs(got["x"][loc] - w["x"][loc]).max() < 1e-12
+    assert np.abs(got["f"][loc] - w["f"][loc]).max() < 1e-9
+    cp.close()
+
+
 def test_pipelined_step_host_matches_oracle(pkg, orc, wl, potentials, gpu_lib):
     """Three pipelined FP64 calls against three oracle loop bodies from the same host state."""
     cells = (9, 9, 9)
