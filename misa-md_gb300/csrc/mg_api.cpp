@@ -1267,7 +1267,7 @@ mg_status mg_clear_errors(mg_context *ctx) {
 // kernels and their order are those of the unpipelined path, so the result is bit-identical to it. If a
 // chunk's decide met a displaced atom that does not go straight back to its own site, the step is void:
 // it runs again in full from the kept input, as mg_upload + one loop body + mg_download would.
-// S in-chunks and SS >= 6 density slabs, SS <= bz / 4, at least 32 sites of a parity per plane.
+// S >= 6 in-chunks and 6 <= SS <= bz / 4 density slabs, at least 32 sites of a parity per plane.
 static mg_status step_host_overlapped(mg_context *ctx, mg_atom_element *atoms, mg_atom_element *inter,
                                       int64_t inter_cap, int64_t *n_inter, int S, int SS) {
     const Geom &g = ctx->g;
@@ -1289,18 +1289,21 @@ static mg_status step_host_overlapped(mg_context *ctx, mg_atom_element *atoms, m
     const int pp = g.by * g.nxh;                               // sites of one parity per local plane
     const size_t rec = sizeof(mg_atom_element);
     size_t ev = 0;
-    // in-chunks of whole planes, the last one thin (4 planes)
+    // in-chunks of whole planes: three thin ones (4 planes) first, so that the first slabs start early,
+    // then even ones, and a thin last one
     auto local_plane_bound = [&](int c) {
         if (c == S) return K;
         if (c == S - 1) return K - 4;
-        return static_cast<int>((static_cast<int64_t>(c) * (K - 4)) / (S - 1));
+        if (c <= 3) return 4 * c;
+        return 12 + static_cast<int>((static_cast<int64_t>(c - 3) * (K - 16)) / (S - 4));
     };
-    // density and force slabs: kb[c] local planes, u[c] sites (whole 32-site groups)
+    // density and force slabs: kb[c] local planes, u[c] sites (whole 32-site groups). Three thin ones at
+    // the bottom and two at the top (4 planes), even ones of at least 4 planes between
     std::vector<int> kb(SS + 1), u(SS + 1);
     for (int c = 0; c <= SS; c++) {
-        if (c <= 2) kb[c] = 4 * c;
+        if (c <= 3) kb[c] = 4 * c;
         else if (c >= SS - 2) kb[c] = K - 4 * (SS - c);
-        else kb[c] = 8 + static_cast<int>((static_cast<int64_t>(c - 2) * (K - 16)) / (SS - 4));
+        else kb[c] = 12 + static_cast<int>((static_cast<int64_t>(c - 3) * (K - 20)) / (SS - 5));
         u[c] = c == SS ? g.n_local_half : static_cast<int>(((static_cast<int64_t>(kb[c]) * pp) >> 5) << 5);
     }
     auto last_plane = [&](int c) { return (u[c + 1] - 1) / pp; };    // the plane of slab c's last site
@@ -1430,8 +1433,10 @@ static mg_status step_host_pipelined(mg_context *ctx, mg_atom_element *atoms, mg
     const Geom &g = ctx->g;
     const int S = std::min(ctx->host_chunks, g.bz);
     {
-        const int SS = std::min(S, g.bz / 4);
-        if (S >= 3 && SS >= 6 && g.by * g.nxh >= 32) return step_host_overlapped(ctx, atoms, inter, inter_cap, n_inter, S, SS);
+        // density slabs about twice as many as the chunks: thinner slabs keep the copies out close
+        // behind the copies in
+        const int SS = std::min(2 * S, g.bz / 4);
+        if (S >= 6 && SS >= 6 && g.by * g.nxh >= 32) return step_host_overlapped(ctx, atoms, inter, inter_cap, n_inter, S, SS);
     }
     if (!ctx->copy_in) MG_CK(cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
     if (!ctx->copy_out) MG_CK(cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));
