@@ -186,9 +186,13 @@ mg_status mg_clear_errors(mg_context *ctx);
  * being the state of record, as in the reference's host loop. Device errors of the step are
  * returned (MG_ERR_CAPACITY, ...).
  * One loop body with a fixed dt and no inter atoms in (*n_inter == 0) is pipelined: the slot array
- * moves in z-slabs of whole planes, and each slab's copy overlaps the unpack and firststep of the
- * previous one (in) or the force pass of the next one (out). The result is bit-identical to the
- * unpipelined path. With a pinned slot array (mg_host_register) the copies run asynchronously.
+ * moves in z-chunks of whole planes. In boxes of at least 24 planes the density and force slabs run
+ * as their planes arrive and go back out while later chunks still come in. Decide is taken per chunk
+ * for displaced atoms that return to their own site; any other displaced atom makes the call run the
+ * loop body again in full from its kept input (an extra device copy of the slot array). Thinner boxes
+ * overlap the copies in with firststep and the copies out with the force slabs. The result is
+ * bit-identical to the unpipelined path. With a pinned slot array (mg_host_register) the copies run
+ * asynchronously.
  * ------------------------------------------------------------------------------------------- */
 mg_status mg_step_host(mg_context *ctx, mg_atom_element *atoms, int64_t n_slots, mg_atom_element *inter,
                        int64_t inter_cap, int64_t *n_inter, int64_t nsteps);
@@ -199,7 +203,7 @@ mg_status mg_step_host(mg_context *ctx, mg_atom_element *atoms, int64_t n_slots,
  * results are bit-identical either way. mg_run_stages uses the same graph for runs of bodies with
  * no stage event between them. */
 mg_status mg_set_step_fusion(mg_context *ctx, int32_t steps_per_graph);
-/* Number of z-slabs of mg_step_host's pipeline (default 16; 0 or 1: no pipelining). */
+/* Number of z-chunks of mg_step_host's pipeline (default 16; 0 or 1: no pipelining). */
 mg_status mg_set_host_pipeline(mg_context *ctx, int32_t chunks);
 /* Verlet skin of the mixed form's candidate lists, in Angstrom (default 0.2; 0: off; at most a0).
  * Each group of 32 sites keeps the pruned candidates that some site of the group had within
